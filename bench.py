@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 MNAD RTM hot path.
+
+Workload (one "step" = one pass over the batch): batched RTM of the
+1201 x 401 @ 12.5 m Gaussian-random-field model with three dipping
+reflectors, 64 shots every 187.5 m, 20 Hz Ricker, dt = 1 ms, 4 s, BF16
+source snapshots, FP64 image stack -- per shot the reference workflow of
+SRC/migration/main_Acoustic_RTM.m:221-253 (true-model forward, background
+forward with snapshots, scattered data, adjoint with imaging).  Inputs are
+seeded synthetic models (no dataset).
+
+value    : grid-point updates per second over all propagations (Gpts/s),
+           device-timed with CUDA events, inputs resident in HBM.
+e2e      : same metric through the public C ABI (mnad_run_jobs) with host
+           buffers, host<->device copies inside the timed region.
+plain    : the single-shot drop-in path (mnad_fwd_pde_exact x2 +
+           mnad_born_adj per shot, serial), same metric.
+--impl reference : the reference algorithm (literal FP64 sparse-operator
+           restatement) on the host cores, shots in a process pool.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.join(ROOT, "mnad-modeling-rtm_gb300")
+for p in (ROOT, PKG_ROOT):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "RTM shots/hr & MNAD Gpts/s, batched vs plain, rel err ≤1e-4; p99 shot latency"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shots", type=int, default=64)
+    ap.add_argument("--nt", type=int, default=4000)
+    ap.add_argument("--plain-shots", type=int, default=2)
+    ap.add_argument("--no-extras", action="store_true", help="skip e2e, plain and CPU legs")
+    ap.add_argument("--ref-steps", type=int, default=12, help="reference arm: time steps per worker sample")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per point-update of the step kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def barrier_sync(world):
+    import torch
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def allmax(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(sv, seconds=15.0):
+    """C OpenMP FP64 port of the reference algorithm on one shot (bounded)."""
+    import numpy as np
+    from oracle import coracle
+    sh = sv.shots[0]
+    w = sv.w
+    probe = 5
+    t = time.perf_counter()
+    coracle.fwd(sv.dx, sh.xs, sh.xr, sv.dz, sh.zs, sh.zr, sv.v, sv.dt, probe, w, sv.d_pml)
+    per = (time.perf_counter() - t) / probe
+    n = max(probe, min(sv.nt, int(seconds / max(per, 1e-6))))
+    t = time.perf_counter()
+    coracle.fwd(sv.dx, sh.xs, sh.xr, sv.dz, sh.zs, sh.zr, sv.v, sv.dt, n, w, sv.d_pml)
+    el = time.perf_counter() - t
+    pts = float(sv.nz * sv.nx * n)
+    return {"value": pts / el / 1e9, "unit": "Gpts/s", "cores": coracle.threads(), "kind": "port",
+            "sample": f"one forward propagation of {sv.name} shot 0, {n} of {sv.nt} steps "
+                      f"({sv.nz}x{sv.nx} padded), FP64 matrix-free C/OpenMP restatement, {el:.1f} s"}
+
+
+def plain_path(ctx, sv, nshots):
+    """Single-shot drop-in calls, serial: fwd(true), fwd(background, indx=1),
+    scattered data on the host, adjoint (the reference's per-shot calls)."""
+    import numpy as np
+    t = time.perf_counter()
+    for k in range(nshots):
+        sh = sv.shots[k]
+        a = (sv.dx, sh.xs, sh.xr, sv.dz, sh.zs, sh.zr)
+        data = ctx.fwd(*a, sv.v, sv.dt, sv.nt, sv.w, sv.d_pml, ss=k + 1)
+        bg = ctx.fwd(*a, sv.vs, sv.dt, sv.nt, sv.w, sv.d_pml, ss=k + 1, indx=1)
+        ctx.adj(sv.dx, sv.dz, sv.nt, sv.dt, sv.vs, sh.xr, sh.zr, data - bg, sv.d_pml, ss=k + 1)
+        ctx.wavefield_release(k + 1)
+    el = time.perf_counter() - t
+    pts = 3.0 * sv.nz * sv.nx * sv.nt * nshots
+    return {"value": pts / el / 1e9, "unit": "Gpts/s", "shots_per_hr": nshots / el * 3600.0,
+            "shots": nshots, "seconds": el}
+
+
+def run_ours(args):
+    import numpy as np
+    rank, world, local = dist_setup(args.gpus)
+    import mnad
+    from mnad import workflow
+    sv = workflow.config3(seed=rank, nshots=args.shots, nt=args.nt)
+    jobs = workflow.shot_jobs(sv, "rtm")
+    ctx = mnad.Context(local, snapshot_codec=sv.codec)
+    plan = ctx.plan(jobs)
+    for _ in range(max(args.warmup, 0)):
+        plan.run()
+    barrier_sync(world)
+    sampler = ClockSampler(local)
+    sampler.start()
+    run_ms, step_ms = [], []
+    launches = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plan.run()
+        tm = plan.timing()
+        run_ms.append(tm["run_ms"])
+        step_ms.append(tm["step_ms"])
+        launches += tm["step_launches"] + 2 + len(jobs)   # step kernels + source seeding + residuals
+    barrier_sync(world)
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    pts, abytes = plan.work()
+    total_s = allmax(sum(run_ms) / 1e3, world)
+    pts_all = allsum(pts * args.steps, world)
+    value = pts_all / total_s / 1e9
+    ms_per_step = total_s * 1e3 / args.steps
+    shots_hr = allsum(len(jobs) * args.steps, world) / total_s * 3600.0
+    peak, peak_kind = peaks()
+    achieved = abytes * args.steps / (sum(step_ms) / 1e3) / 1e9
+    tr = profile_traffic()
+    traffic = None
+    if tr and "bytes_per_point_update" in tr:
+        traffic = tr["bytes_per_point_update"] * pts / (plan.timing()["step_launches"])
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "peak_kind": f"{peak_kind} hbm_gbs", "kernel": "mnad::step_direct",
+            "algorithmic_bytes_per_launch": abytes / plan.timing()["step_launches"]}
+    plan.close()
+    extras = {}
+    if not args.no_extras:
+        # e2e through the C ABI with host buffers (upload, run, download inside)
+        for j in jobs:
+            j.image[:] = 0
+        h0, d0 = ctx.transfers()
+        barrier_sync(world)
+        t = time.perf_counter()
+        ctx.run_jobs(jobs)
+        e2e_s = time.perf_counter() - t
+        h1, d1 = ctx.transfers()
+        e2e_s = allmax(e2e_s, world)
+        extras["e2e"] = {"value": round(allsum(pts, world) / e2e_s / 1e9, 3), "unit": "Gpts/s",
+                         "h2d_bytes_per_step": int(h1 - h0), "d2h_bytes_per_step": int(d1 - d0),
+                         "shots_per_hr": round(allsum(len(jobs), world) / e2e_s * 3600.0, 1),
+                         "api": "mnad_run_jobs"}
+        if rank == 0 and args.plain_shots > 0:
+            extras["plain"] = plain_path(ctx, sv, args.plain_shots)
+            extras["plain"]["value"] = round(extras["plain"]["value"], 3)
+        if rank == 0:
+            extras["cpu_baseline"] = cpu_baseline(sv)
+    ctx.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": "Gpts/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 2),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded Gaussian random field + dipping reflectors)",
+                "config": {"workload": "batched RTM, config 3", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
+                           "shots": len(jobs), "nt": sv.nt, "dt": sv.dt, "propagations_per_shot": 3,
+                           "snapshots": sv.codec, "image": "f64", "parallelism": f"replicas x{world}",
+                           "l2": "state per step >> L2 (inputs larger than L2)"},
+                "shots_per_hr": round(shots_hr, 1), "roofline": roof, "clocks": clocks,
+                "gpu_launches": launches, "wall_s": round(wall, 2)}
+        line.update(extras)
+        if "plain" in extras:
+            line["batched_vs_plain"] = round(value / extras["plain"]["value"], 2)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+_REF = {}
+
+
+def _ref_init(seed, nshots, nt):
+    from mnad import workflow
+    from oracle import mnad_oracle as P
+    sv = workflow.config3(seed=seed, nshots=nshots, nt=nt)
+    _REF["sv"] = sv
+    _REF["A"] = P.a_gen(sv.dx, sv.dz, sv.dt, sv.v)
+
+
+def _ref_shot(args):
+    k, nsteps = args
+    from oracle import mnad_oracle as P
+    sv = _REF["sv"]
+    sh = sv.shots[k % len(sv.shots)]
+    t = time.perf_counter()
+    P.fwd_pde_exact_mnad(sv.dx, sh.xs, sh.xr, sv.dz, sh.zs, sh.zr, sv.v, sv.dt, nsteps, sv.w, sv.d_pml,
+                         A=_REF["A"])
+    return time.perf_counter() - t, float(sv.nz * sv.nx * nsteps)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    workers = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers, initializer=_ref_init, initargs=(0, args.shots, args.nt)) as pool:
+        tasks = [(k, args.ref_steps) for k in range(workers)]
+        for _ in range(max(args.warmup, 0)):
+            pool.map(_ref_shot, [(k, 1) for k in range(workers)])
+        vals = []
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            res = pool.map(_ref_shot, tasks)
+            el = time.perf_counter() - t
+            vals.append(sum(r[1] for r in res) / el / 1e9)
+        wall = time.perf_counter() - t0
+    value = statistics.median(vals)
+    sample = (f"{workers} worker processes (parfor analogue), each one shot of config 3 for {args.ref_steps} "
+              f"time steps (401x1201 + 2x40 CPML), literal FP64 sparse-operator restatement (SciPy)")
+    line = {"metric": METRIC, "value": round(value, 5), "unit": "Gpts/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(wall * 1e3 / args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gaussian random field + dipping reflectors)",
+            "config": {"workload": "batched RTM, config 3", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
+                       "shots": args.shots, "nt": args.nt, "parallelism": f"{workers} host processes"},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 5), "unit": "Gpts/s", "cores": workers, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 5), "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

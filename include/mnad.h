@@ -1,0 +1,196 @@
+/*
+ * mnad.h -- C ABI of the GB300 MNAD modeling / RTM library (libmnad.so).
+ *
+ * The library runs the time-stepping hot path of the MNAD acoustic modeling
+ * and reverse-time-migration code on one NVIDIA GB300 (sm_103a): the fused
+ * MNAD compact-stencil update of U and its gradient fields V = U_x, W = U_z
+ * under CPML, source injection, receiver sampling, d2u snapshots with
+ * illumination, and the adjoint propagation with the zero-lag
+ * cross-correlation imaging condition.
+ *
+ * Conventions (those of the reference MATLAB code):
+ *   - grids are the PML-padded nz x nx model, column-major (z fastest);
+ *   - source/receiver positions are 1-based padded grid indices, passed as
+ *     doubles that must hold integer values (the MATLAB drivers compute them
+ *     as d_pml + metres/dx);
+ *   - receiver data is nt x nr column-major FP64 (datau(tt, rr));
+ *   - images and illumination are (nz-2*d_pml) x (nx-2*d_pml) column-major
+ *     FP64 (the reference's Nint x 1 vectors).
+ *
+ * Every function returns an int status (MNAD_OK == 0).  On failure
+ * mnad_last_error() returns a message for the calling thread.  Functions
+ * taking a context may be called from several threads only if each thread
+ * uses its own context.
+ */
+#ifndef MNAD_H
+#define MNAD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MNAD_API __attribute__((visibility("default")))
+#else
+#define MNAD_API
+#endif
+
+#define MNAD_ABI_VERSION 1
+
+/* Status codes. */
+enum {
+    MNAD_OK = 0,
+    MNAD_E_ARG = 1,        /* invalid argument (sizes, indices, T, ...) */
+    MNAD_E_OOM = 2,        /* device or host allocation failed */
+    MNAD_E_CUDA = 3,       /* CUDA runtime/driver error */
+    MNAD_E_TIMEOUT = 4,    /* a bounded device wait ran out */
+    MNAD_E_NOTFOUND = 5,   /* no stored source wavefield for this shot id */
+    MNAD_E_NUMERIC = 6,    /* non-finite values / codec saturation detected */
+    MNAD_E_BUDGET = 7,     /* job does not fit the context's HBM budget */
+    MNAD_E_STATE = 8       /* call not valid in the current state */
+};
+
+/* Storage codec of the source-side d2u snapshots. */
+enum { MNAD_SNAP_F32 = 0, MNAD_SNAP_BF16 = 1, MNAD_SNAP_F16 = 2 };
+
+/* Snapshot pairing of the imaging condition.
+ * REFERENCE: column ncols-ttt+1 of UU, ncols = max(2*nf+1, k) as in
+ *            SRC/migration/Born_adj_MNAD.m:128 (columns past k are zero).
+ * ALIGNED:   column k-ttt+1 (source and receiver fields at the same time). */
+enum { MNAD_PAIR_REFERENCE = 0, MNAD_PAIR_ALIGNED = 1 };
+
+/* Step kernel choice. */
+enum { MNAD_KERNEL_AUTO = 0, MNAD_KERNEL_DIRECT = 1, MNAD_KERNEL_TMA = 2 };
+
+typedef struct mnad_options {
+    int snapshot_codec;   /* MNAD_SNAP_*; default MNAD_SNAP_F32 */
+    int pairing;          /* MNAD_PAIR_*; default MNAD_PAIR_REFERENCE */
+    int T;                /* snapshot interval; <= 0: reference formula
+                             T = floor(nt/nf/2), nf = floor(nt/(6 vmax/vmin))
+                             (SRC/MNAD/fwd_PDE_exact_MNAD.m:46-47) */
+    int record_vw;        /* forward also records V and W (reference keeps
+                             them commented out, fwd_PDE_exact_MNAD.m:167-168) */
+    int use_graphs;       /* capture the time loop in a CUDA graph (default 1) */
+    int kernel;           /* MNAD_KERNEL_*; default AUTO */
+} mnad_options;
+
+typedef struct mnad_context mnad_context;
+
+/* ---- context ---------------------------------------------------------- */
+MNAD_API int mnad_abi_version(void);
+MNAD_API const char* mnad_last_error(void);
+/* Creates a context on CUDA device `device` with its own stream.
+ * hbm_budget_bytes bounds the device memory the context keeps for job
+ * state and stored wavefields (0: no bound). */
+MNAD_API int mnad_context_create(int device, size_t hbm_budget_bytes, mnad_context** out);
+MNAD_API int mnad_context_destroy(mnad_context* ctx);
+MNAD_API int mnad_context_set_options(mnad_context* ctx, const mnad_options* opt);
+MNAD_API int mnad_context_get_options(const mnad_context* ctx, mnad_options* opt);
+/* Bytes of device memory currently held by the context (state + wavefields). */
+MNAD_API int mnad_context_memory(const mnad_context* ctx, size_t* bytes_in_use);
+/* Host<->device bytes the context has copied so far (inputs, outputs). */
+MNAD_API int mnad_context_transfers(const mnad_context* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
+/* Bit set of device-side status flags seen so far (and clears them). */
+MNAD_API int mnad_context_status(mnad_context* ctx, unsigned* flags);
+
+/* ---- drop-in entry points (reference call signatures) ------------------- */
+
+/* data = fwd_PDE_exact_MNAD(dx,xs,xr,dz,zs,zr,v,dt,nt,w,d_pml,ss,Auu,...,Aww,indx)
+ * (SRC/MNAD/fwd_PDE_exact_MNAD.m:1).  The nine sparse operators are
+ * deterministic functions of (v, dx, dz, dt) and are recomputed on the
+ * device, so they are not passed.  datau receives nt x nr (data{1}).
+ * datav/dataw may be NULL; when non-NULL (and options.record_vw set) they
+ * receive the V/W receiver traces.  With indx == 1 the d2u snapshots and the
+ * illumination are kept on the device under shot id `ss` (replacing
+ * ./Wavefields/UU_<ss>.mat and ./Illuminations/illum_<ss>.mat, :160-164). */
+MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const double* xr, int nr,
+                                double dz, double zs, const double* zr,
+                                const double* v, int nz, int nx, double dt, int nt,
+                                const double* w, int d_pml, int ss, int indx,
+                                double* datau, double* datav, double* dataw);
+
+/* Forward modeling as mnad_fwd_pde_exact(..., indx=0) that also returns the
+ * wavefields after the listed steps: for each 1-based step steps[k]
+ * (ascending, 1..nt), fields receives nU, nV, nW of that step
+ * (SRC/MNAD/fwd_PDE_exact_MNAD.m:114-116) as 3 consecutive nz x nx
+ * column-major FP64 arrays (nkeep*3*nz*nx values in total). */
+MNAD_API int mnad_fwd_fields(mnad_context* ctx, double dx, double xs, const double* xr, int nr,
+                             double dz, double zs, const double* zr,
+                             const double* v, int nz, int nx, double dt, int nt,
+                             const double* w, int d_pml, int nkeep, const int* steps,
+                             double* datau, double* fields);
+
+/* Im = Born_adj_MNAD(dx,dz,nt,dt,v,xr,zr,data,d_pml,ss,Auu,...,Aww)
+ * (SRC/migration/Born_adj_MNAD.m:1).  data is the nt x nr residual
+ * (data{1} of the reference, :50); the source wavefield of shot `ss` must
+ * have been stored by mnad_fwd_pde_exact(..., indx=1) or
+ * mnad_wavefield_import().  im receives the Nint image, already multiplied
+ * by T (:138). */
+MNAD_API int mnad_born_adj(mnad_context* ctx, double dx, double dz, int nt, double dt,
+                           const double* v, int nz, int nx, const double* xr, const double* zr, int nr,
+                           const double* data, int d_pml, int ss, double* im);
+
+/* ---- stored source wavefields (the ./Wavefields hand-off) -------------- */
+/* nint = (nz-2d)(nx-2d); ncols = columns of the reference's UU matrix;
+ * nsnap = columns actually filled (k = floor(nt/T)); T = snapshot interval. */
+MNAD_API int mnad_wavefield_info(mnad_context* ctx, int ss, int64_t* nint, int* ncols, int* nsnap, int* T);
+/* UU: nint x ncols FP64 (columns past nsnap are zero, as in the reference's
+ * preallocated matrix); illum: nint FP64, times T.  Either may be NULL. */
+MNAD_API int mnad_wavefield_export(mnad_context* ctx, int ss, double* UU, double* illum);
+/* Stores a UU matrix loaded from UU_<ss>.mat (parfor may run a shot's
+ * forward and adjoint in different processes).  illum may be NULL. */
+MNAD_API int mnad_wavefield_import(mnad_context* ctx, int ss, int nz, int nx, int d_pml, int nt, int T,
+                                   int ncols, int nsnap, const double* UU, const double* illum);
+MNAD_API int mnad_wavefield_release(mnad_context* ctx, int ss);
+
+/* ---- batched jobs (many shots per launch) ----------------------------- */
+enum { MNAD_JOB_MODEL = 0, MNAD_JOB_RTM = 1 };
+
+typedef struct mnad_job {
+    int kind;                 /* MNAD_JOB_MODEL or MNAD_JOB_RTM */
+    int nz, nx, d_pml, nt;    /* padded grid, CPML thickness, steps */
+    double dx, dz, dt;
+    const double* v;          /* true model, nz*nx column-major (host) */
+    const double* vs;         /* RTM: migration (background) model */
+    double zs, xs;            /* 1-based padded source indices */
+    int nr;
+    const double* zr;         /* 1-based padded receiver indices [nr] */
+    const double* xr;
+    const double* w;          /* source wavelet [nt] */
+    int T;                    /* RTM snapshot interval, <= 0: formula on vs */
+    double* data_out;         /* MODEL: shot gather nt x nr; RTM: scattered
+                                 data data - datas (may be NULL) */
+    double* image_out;        /* RTM: Nint image, times T */
+    double* illum_out;        /* RTM: Nint illumination, times T (may be NULL) */
+} mnad_job;
+
+/* Runs the jobs as batches of propagations advancing together (one launch
+ * per time step for every shot of a phase): MODEL = one forward; RTM = the
+ * reference workflow of SRC/migration/main_Acoustic_RTM.m:221-253 per shot
+ * (true-model forward, background forward with snapshots, scattered data
+ * formed on the device, adjoint with imaging).  Host buffers in, host
+ * buffers out. */
+MNAD_API int mnad_run_jobs(mnad_context* ctx, const mnad_job* jobs, int njobs);
+
+/* Device-resident form of mnad_run_jobs: create uploads every input and
+ * allocates all state; run executes all phases on the device; download
+ * copies the outputs into the jobs' host pointers. */
+typedef struct mnad_plan mnad_plan;
+MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs, mnad_plan** out);
+MNAD_API int mnad_plan_run(mnad_plan* plan);
+MNAD_API int mnad_plan_download(mnad_plan* plan);
+MNAD_API int mnad_plan_destroy(mnad_plan* plan);
+/* Grid-point updates one run performs (sum over propagations of nz*nx*nt)
+ * and the algorithmic HBM bytes of those updates. */
+MNAD_API int mnad_plan_work(const mnad_plan* plan, double* point_updates, double* algorithmic_bytes);
+/* Device time of the last run (ms, CUDA events on the plan's stream) and the
+ * device time spent in step kernels only. */
+MNAD_API int mnad_plan_timing(const mnad_plan* plan, double* run_ms, double* step_ms, int* step_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MNAD_H */

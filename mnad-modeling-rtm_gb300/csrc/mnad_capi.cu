@@ -1,0 +1,628 @@
+// C ABI of libmnad.so (declared in include/mnad.h).
+#include "mnad_engine.h"
+#include "mnad_kernels.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+using namespace mnad;
+
+struct mnad_context : Context {
+    using Context::Context;
+};
+
+static thread_local std::string g_err;
+
+template <class F>
+static int guard(F&& f)
+{
+    try {
+        f();
+        return MNAD_OK;
+    } catch (const Error& e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_err = "host allocation failed";
+        return MNAD_E_OOM;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return MNAD_E_CUDA;
+    }
+}
+
+static void need(bool ok, const std::string& msg)
+{
+    if (!ok) throw Error(MNAD_E_ARG, msg);
+}
+
+// 1-based grid index passed as a double (MATLAB) -> 0-based int.
+static int index1(double x, int n, const char* what)
+{
+    need(std::isfinite(x) && x == std::floor(x) && x >= 1 && x <= n,
+         std::string(what) + " must be an integer grid index in [1, " + std::to_string(n) + "], got " + std::to_string(x));
+    return (int)x - 1;
+}
+
+static void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, const double* v)
+{
+    need(v != nullptr, "v is NULL");
+    need(nz >= 1 && nx >= 1, "grid must be at least 1 x 1");
+    need(d >= 0 && nz >= 2 * d && nx >= 2 * d, "d_pml must satisfy 0 <= 2*d_pml <= min(nz, nx) (C_cof.m builds the strips)");
+    need(nt >= 1, "nt must be >= 1");
+    need(std::isfinite(dx) && dx > 0 && std::isfinite(dz) && dz > 0 && std::isfinite(dt) && dt > 0,
+         "dx, dz, dt must be positive and finite");
+    const size_t n = (size_t)nz * nx;
+    for (size_t k = 0; k < n; ++k)
+        need(std::isfinite(v[k]) && v[k] > 0, "velocity must be positive and finite (entry " + std::to_string(k) + ")");
+}
+
+static bool use_graph(const Context& c, int nt) { return c.opt.use_graphs != 0 && nt >= 1; }
+
+extern "C" {
+
+MNAD_API int mnad_abi_version(void) { return MNAD_ABI_VERSION; }
+
+MNAD_API const char* mnad_last_error(void) { return g_err.c_str(); }
+
+MNAD_API int mnad_context_create(int device, size_t hbm_budget_bytes, mnad_context** out)
+{
+    return guard([&] {
+        need(out != nullptr, "out is NULL");
+        *out = nullptr;
+        int n = 0;
+        MNAD_CK(cudaGetDeviceCount(&n));
+        need(device >= 0 && device < n, "no CUDA device " + std::to_string(device));
+        *out = new mnad_context(device, hbm_budget_bytes);
+    });
+}
+
+MNAD_API int mnad_context_destroy(mnad_context* ctx)
+{
+    return guard([&] { delete ctx; });
+}
+
+MNAD_API int mnad_context_set_options(mnad_context* ctx, const mnad_options* o)
+{
+    return guard([&] {
+        need(ctx && o, "NULL argument");
+        need(o->snapshot_codec == MNAD_SNAP_F32 || o->snapshot_codec == MNAD_SNAP_BF16,
+             "snapshot_codec must be MNAD_SNAP_F32 or MNAD_SNAP_BF16");
+        need(o->pairing == MNAD_PAIR_REFERENCE || o->pairing == MNAD_PAIR_ALIGNED, "bad pairing");
+        need(o->kernel >= MNAD_KERNEL_AUTO && o->kernel <= MNAD_KERNEL_TMA, "bad kernel");
+        ctx->opt = *o;
+    });
+}
+
+MNAD_API int mnad_context_get_options(const mnad_context* ctx, mnad_options* o)
+{
+    return guard([&] {
+        need(ctx && o, "NULL argument");
+        *o = ctx->opt;
+    });
+}
+
+MNAD_API int mnad_context_memory(const mnad_context* ctx, size_t* bytes)
+{
+    return guard([&] {
+        need(ctx && bytes, "NULL argument");
+        *bytes = ctx->in_use;
+    });
+}
+
+MNAD_API int mnad_context_transfers(const mnad_context* ctx, uint64_t* h2d, uint64_t* d2h)
+{
+    return guard([&] {
+        need(ctx != nullptr, "context is NULL");
+        if (h2d) *h2d = ctx->h2d;
+        if (d2h) *d2h = ctx->d2h;
+    });
+}
+
+MNAD_API int mnad_context_status(mnad_context* ctx, unsigned* flags)
+{
+    return guard([&] {
+        need(ctx && flags, "NULL argument");
+        MNAD_CK(cudaSetDevice(ctx->device));
+        *flags = ctx->take_status();
+    });
+}
+
+// ---------------------------------------------------------------------------
+static std::unique_ptr<Wavefield> new_wavefield(Context& c, int nz, int nx, int d, int nt, int T, int ncols,
+                                                int nsnap, int codec)
+{
+    auto wf = std::make_unique<Wavefield>();
+    wf->nz = nz; wf->nx = nx; wf->d = d; wf->nt = nt; wf->T = T;
+    wf->ncols = ncols; wf->nsnap = nsnap; wf->codec = codec;
+    wf->nint = (size_t)(nz - 2 * d) * (nx - 2 * d);
+    const size_t cb = codec == MNAD_SNAP_F32 ? 4 : 2;
+    wf->snap = DevMem(&c, std::max<size_t>(1, wf->nint * (size_t)nsnap * cb));
+    wf->illum = DevMem(&c, std::max<size_t>(1, wf->nint * sizeof(double)));
+    MNAD_CK(cudaMemsetAsync(wf->illum.get(), 0, wf->illum.size(), c.stream));
+    if (codec == MNAD_SNAP_F16) {
+        wf->scale = DevMem(&c, std::max(1, nsnap) * sizeof(float));
+        std::vector<float> one(std::max(1, nsnap), 1.0f);
+        upload(c, wf->scale.get(), one.data(), one.size() * sizeof(float));
+    }
+    return wf;
+}
+
+static void fill_receivers(PropSpec& s, const double* xr, const double* zr, int nr)
+{
+    need(nr >= 0, "nr must be >= 0");
+    need(nr == 0 || (xr && zr), "receiver index arrays are NULL");
+    s.zr.resize(nr);
+    s.xr.resize(nr);
+    for (int k = 0; k < nr; ++k) {
+        s.zr[k] = index1(zr[k], s.nz, "zr");
+        s.xr[k] = index1(xr[k], s.nx, "xr");
+    }
+}
+
+MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const double* xr, int nr,
+                                double dz, double zs, const double* zr,
+                                const double* v, int nz, int nx, double dt, int nt,
+                                const double* w, int d_pml, int ss, int indx,
+                                double* datau, double* datav, double* dataw)
+{
+    return guard([&] {
+        need(ctx != nullptr, "context is NULL");
+        check_grid(nz, nx, d_pml, nt, dx, dz, dt, v);
+        need(w != nullptr, "w is NULL");
+        need(nr == 0 || datau != nullptr, "datau is NULL");
+        need(indx == 0 || indx == 1, "indx must be 0 or 1");
+        Context& c = *ctx;
+        MNAD_CK(cudaSetDevice(c.device));
+        PropSpec s;
+        s.mode = MODE_FWD;
+        s.nz = nz; s.nx = nx; s.d = d_pml; s.nt = nt;
+        s.dx = dx; s.dz = dz; s.dt = dt; s.v = v; s.w = w;
+        s.zs = index1(zs, nz, "zs");
+        s.xs = index1(xs, nx, "xs");
+        fill_receivers(s, xr, zr, nr);
+        s.record_vw = c.opt.record_vw && (datav || dataw);
+        std::unique_ptr<Wavefield> wf;
+        if (indx == 1) {
+            double vmin, vmax;
+            model_minmax(v, (size_t)nz * nx, vmin, vmax);
+            const int nf = snapshot_nf(nt, vmin, vmax);                     // :46
+            const int T = c.opt.T > 0 ? c.opt.T : snapshot_T(nt, nf);       // :47
+            const int k = nt / T;
+            wf = new_wavefield(c, nz, nx, d_pml, nt, T, std::max(2 * nf + 1, k), k, c.opt.snapshot_codec);
+            s.T = T;
+            s.wf = wf.get();
+        }
+        Prop p;
+        p.spec = s;
+        const TileCfg tc = tile_cfg(c.opt.kernel);
+        p.build(c, tc);
+        Batch b(c, tc);
+        b.add(&p);
+        b.finalize();
+        b.run(use_graph(c, nt));
+        const size_t nd = (size_t)nt * nr;
+        download(c, datau, p.data.get(), nd * sizeof(double));
+        if (s.record_vw && datav) download(c, datav, p.datav.get(), nd * sizeof(double));
+        if (s.record_vw && dataw) download(c, dataw, p.dataw.get(), nd * sizeof(double));
+        c.sync();
+        if (wf) c.wavefields[ss] = std::move(wf);
+    });
+}
+
+MNAD_API int mnad_fwd_fields(mnad_context* ctx, double dx, double xs, const double* xr, int nr,
+                             double dz, double zs, const double* zr,
+                             const double* v, int nz, int nx, double dt, int nt,
+                             const double* w, int d_pml, int nkeep, const int* steps,
+                             double* datau, double* fields)
+{
+    return guard([&] {
+        need(ctx != nullptr, "context is NULL");
+        check_grid(nz, nx, d_pml, nt, dx, dz, dt, v);
+        need(w != nullptr, "w is NULL");
+        need(nr == 0 || datau != nullptr, "datau is NULL");
+        need(nkeep >= 0 && (nkeep == 0 || (steps && fields)), "steps/fields are NULL");
+        for (int k = 0; k < nkeep; ++k)
+            need(steps[k] >= 1 && steps[k] <= nt && (k == 0 || steps[k] > steps[k - 1]),
+                 "steps must be ascending within 1..nt");
+        Context& c = *ctx;
+        MNAD_CK(cudaSetDevice(c.device));
+        PropSpec s;
+        s.mode = MODE_FWD;
+        s.nz = nz; s.nx = nx; s.d = d_pml; s.nt = nt;
+        s.dx = dx; s.dz = dz; s.dt = dt; s.v = v; s.w = w;
+        s.zs = index1(zs, nz, "zs");
+        s.xs = index1(xs, nx, "xs");
+        fill_receivers(s, xr, zr, nr);
+        Prop p;
+        p.spec = s;
+        const TileCfg tc = tile_cfg(c.opt.kernel);
+        p.build(c, tc);
+        Batch b(c, tc);
+        b.add(&p);
+        b.finalize();
+        b.start();
+        const size_t N = (size_t)nz * nx;
+        const double vs = v[(size_t)s.zs + (size_t)s.xs * nz];
+        const double rs = (vs * vs) * (dt * dt);
+        DevMem tmp(&c, N * sizeof(double));
+        int done = 0;
+        for (int k = 0; k < nkeep; ++k) {
+            b.advance(done, steps[k]);
+            done = steps[k];
+            // After step tt the new fields sit in time level tt & 1; the stored
+            // U at the source already holds the injection of step tt+1.
+            const int lvl = done & 1;
+            const float fix = done < nt ? (float)(rs * w[done]) : 0.0f;
+            for (int f = 0; f < 3; ++f) {
+                field_export<<<(int)std::min<size_t>((N + 255) / 256, 4096), 256, 0, c.stream>>>(
+                    p.desc.fld[lvl][f], nz, nx, p.desc.ld, f == 0 ? p.desc.src : -1, f == 0 ? fix : 0.0f,
+                    tmp.as<double>());
+                MNAD_CK(cudaGetLastError());
+                download(c, fields + ((size_t)k * 3 + f) * N, tmp.get(), N * sizeof(double));
+            }
+        }
+        b.advance(done, nt);
+        download(c, datau, p.data.get(), (size_t)nt * nr * sizeof(double));
+        c.sync();
+    });
+}
+
+MNAD_API int mnad_born_adj(mnad_context* ctx, double dx, double dz, int nt, double dt,
+                           const double* v, int nz, int nx, const double* xr, const double* zr, int nr,
+                           const double* data, int d_pml, int ss, double* im)
+{
+    return guard([&] {
+        need(ctx != nullptr, "context is NULL");
+        check_grid(nz, nx, d_pml, nt, dx, dz, dt, v);
+        need(im != nullptr, "im is NULL");
+        need(nr == 0 || data != nullptr, "data is NULL");
+        Context& c = *ctx;
+        MNAD_CK(cudaSetDevice(c.device));
+        auto it = c.wavefields.find(ss);
+        if (it == c.wavefields.end())
+            throw Error(MNAD_E_NOTFOUND, "no stored source wavefield for shot " + std::to_string(ss) +
+                                             " (run the forward with indx=1 or import UU first)");
+        Wavefield& wf = *it->second;
+        need(wf.nint == (size_t)(nz - 2 * d_pml) * (nx - 2 * d_pml),
+             "stored wavefield of shot " + std::to_string(ss) + " has a different interior size");
+        double vmin, vmax;
+        model_minmax(v, (size_t)nz * nx, vmin, vmax);
+        const int T = c.opt.T > 0 ? c.opt.T : snapshot_T(nt, snapshot_nf(nt, vmin, vmax));   // :41-42
+        need(nt / T <= wf.ncols, "more imaging steps (floor(nt/T)) than snapshot columns; "
+                                 "UU(:,end-ttt+1) would index column < 1");
+        PropSpec s;
+        s.mode = MODE_ADJ;
+        s.nz = nz; s.nx = nx; s.d = d_pml; s.nt = nt;
+        s.dx = dx; s.dz = dz; s.dt = dt; s.v = v;
+        fill_receivers(s, xr, zr, nr);
+        s.T = T;
+        s.wf = &wf;
+        s.pairing = c.opt.pairing;
+        Prop p;
+        p.spec = s;
+        const TileCfg tc = tile_cfg(c.opt.kernel);
+        p.build(c, tc);
+        upload(c, p.data.get(), data, (size_t)nt * nr * sizeof(double));
+        Batch b(c, tc);
+        b.add(&p);
+        b.finalize();
+        b.run(use_graph(c, nt));
+        const size_t n = p.nint();
+        DevMem out(&c, n * sizeof(double));
+        scale_f64<<<(int)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c.stream>>>(p.image.as<double>(), (double)T, n,
+                                                                                        out.as<double>());
+        MNAD_CK(cudaGetLastError());
+        download(c, im, out.get(), n * sizeof(double));   // Im = T*Im (:138)
+        c.sync();
+    });
+}
+
+// ---------------------------------------------------------------------------
+MNAD_API int mnad_wavefield_info(mnad_context* ctx, int ss, int64_t* nint, int* ncols, int* nsnap, int* T)
+{
+    return guard([&] {
+        need(ctx != nullptr, "context is NULL");
+        auto it = ctx->wavefields.find(ss);
+        if (it == ctx->wavefields.end()) throw Error(MNAD_E_NOTFOUND, "no stored wavefield for shot " + std::to_string(ss));
+        const Wavefield& wf = *it->second;
+        if (nint) *nint = (int64_t)wf.nint;
+        if (ncols) *ncols = wf.ncols;
+        if (nsnap) *nsnap = wf.nsnap;
+        if (T) *T = wf.T;
+    });
+}
+
+MNAD_API int mnad_wavefield_export(mnad_context* ctx, int ss, double* UU, double* illum)
+{
+    return guard([&] {
+        need(ctx != nullptr, "context is NULL");
+        Context& c = *ctx;
+        MNAD_CK(cudaSetDevice(c.device));
+        auto it = c.wavefields.find(ss);
+        if (it == c.wavefields.end()) throw Error(MNAD_E_NOTFOUND, "no stored wavefield for shot " + std::to_string(ss));
+        const Wavefield& wf = *it->second;
+        if (UU) {
+            const size_t n = wf.nint * (size_t)wf.ncols;
+            DevMem tmp(&c, std::max<size_t>(1, n * sizeof(double)));
+            snap_export<<<(int)std::min<size_t>((n + 255) / 256, 8192), 256, 0, c.stream>>>(
+                wf.snap.get(), wf.codec, wf.scale.as<float>(), wf.nint, wf.nsnap, wf.ncols, tmp.as<double>());
+            MNAD_CK(cudaGetLastError());
+            download(c, UU, tmp.get(), n * sizeof(double));
+            c.sync();
+        }
+        if (illum) {
+            const size_t n = wf.nint;
+            DevMem tmp(&c, std::max<size_t>(1, n * sizeof(double)));
+            scale_f64<<<(int)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c.stream>>>(
+                wf.illum.as<double>(), (double)wf.T, n, tmp.as<double>());   // illum = T*illum (:162)
+            MNAD_CK(cudaGetLastError());
+            download(c, illum, tmp.get(), n * sizeof(double));
+            c.sync();
+        }
+    });
+}
+
+MNAD_API int mnad_wavefield_import(mnad_context* ctx, int ss, int nz, int nx, int d_pml, int nt, int T,
+                                   int ncols, int nsnap, const double* UU, const double* illum)
+{
+    return guard([&] {
+        need(ctx != nullptr && UU != nullptr, "NULL argument");
+        need(nz >= 1 && nx >= 1 && d_pml >= 0 && nz >= 2 * d_pml && nx >= 2 * d_pml, "bad grid");
+        need(T >= 1 && nt >= 1, "T and nt must be >= 1");
+        need(nsnap >= 0 && nsnap <= ncols, "need 0 <= nsnap <= ncols");
+        Context& c = *ctx;
+        MNAD_CK(cudaSetDevice(c.device));
+        auto wf = new_wavefield(c, nz, nx, d_pml, nt, T, ncols, nsnap, c.opt.snapshot_codec);
+        const size_t n = wf->nint * (size_t)nsnap;
+        if (n) {
+            DevMem tmp(&c, n * sizeof(double));
+            upload(c, tmp.get(), UU, n * sizeof(double));
+            snap_import<<<(int)std::min<size_t>((n + 255) / 256, 8192), 256, 0, c.stream>>>(
+                tmp.as<double>(), wf->codec, wf->scale.as<float>(), wf->nint, nsnap, wf->snap.get());
+            MNAD_CK(cudaGetLastError());
+            c.sync();
+        }
+        if (illum) {
+            DevMem tmp(&c, wf->nint * sizeof(double));
+            upload(c, tmp.get(), illum, wf->nint * sizeof(double));
+            scale_f64<<<(int)std::min<size_t>((wf->nint + 255) / 256, 4096), 256, 0, c.stream>>>(
+                tmp.as<double>(), 1.0 / T, wf->nint, wf->illum.as<double>());
+            MNAD_CK(cudaGetLastError());
+            c.sync();
+        }
+        c.wavefields[ss] = std::move(wf);
+    });
+}
+
+MNAD_API int mnad_wavefield_release(mnad_context* ctx, int ss)
+{
+    return guard([&] {
+        need(ctx != nullptr, "context is NULL");
+        auto it = ctx->wavefields.find(ss);
+        if (it == ctx->wavefields.end()) throw Error(MNAD_E_NOTFOUND, "no stored wavefield for shot " + std::to_string(ss));
+        MNAD_CK(cudaSetDevice(ctx->device));
+        ctx->wavefields.erase(it);
+        ctx->sync();
+    });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched jobs.
+struct mnad_plan {
+    mnad_context* ctx = nullptr;
+    std::vector<mnad_job> jobs;
+    std::vector<std::unique_ptr<Prop>> props;            // owns every propagation
+    std::vector<Prop*> fwd_true, fwd_bg, adj;            // per job (nullptr where not used)
+    std::vector<std::unique_ptr<Wavefield>> wfs;
+    std::unique_ptr<Batch> phase1, phase3;
+    cudaEvent_t ev[4] = {};
+    double pts = 0, bytes = 0;
+    float run_ms = 0, step_ms = 0;
+    int launches = 0;
+    ~mnad_plan()
+    {
+        if (ctx) cudaStreamSynchronize(ctx->stream);
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+static void check_job(const mnad_job& j, int k)
+{
+    const std::string pre = "job " + std::to_string(k) + ": ";
+    need(j.kind == MNAD_JOB_MODEL || j.kind == MNAD_JOB_RTM, pre + "kind must be MNAD_JOB_MODEL or MNAD_JOB_RTM");
+    check_grid(j.nz, j.nx, j.d_pml, j.nt, j.dx, j.dz, j.dt, j.v);
+    need(j.w != nullptr, pre + "w is NULL");
+    if (j.kind == MNAD_JOB_RTM) {
+        check_grid(j.nz, j.nx, j.d_pml, j.nt, j.dx, j.dz, j.dt, j.vs);
+        need(j.image_out != nullptr, pre + "image_out is NULL");
+    } else {
+        need(j.nr == 0 || j.data_out != nullptr, pre + "data_out is NULL");
+    }
+}
+
+static Prop* add_prop(mnad_plan& P, const mnad_job& j, int mode, const double* v, Wavefield* wf, int T)
+{
+    auto p = std::make_unique<Prop>();
+    PropSpec& s = p->spec;
+    s.mode = mode;
+    s.nz = j.nz; s.nx = j.nx; s.d = j.d_pml; s.nt = j.nt;
+    s.dx = j.dx; s.dz = j.dz; s.dt = j.dt; s.v = v; s.w = j.w;
+    if (mode == MODE_FWD) {
+        s.zs = index1(j.zs, j.nz, "zs");
+        s.xs = index1(j.xs, j.nx, "xs");
+    }
+    fill_receivers(s, j.xr, j.zr, j.nr);
+    s.wf = wf;
+    s.T = T;
+    s.pairing = P.ctx->opt.pairing;
+    P.props.push_back(std::move(p));
+    return P.props.back().get();
+}
+
+extern "C" {
+
+MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs, mnad_plan** out)
+{
+    return guard([&] {
+        need(ctx && out && (njobs == 0 || jobs), "NULL argument");
+        need(njobs >= 0, "njobs must be >= 0");
+        *out = nullptr;
+        Context& c = *ctx;
+        MNAD_CK(cudaSetDevice(c.device));
+        auto P = std::make_unique<mnad_plan>();
+        P->ctx = ctx;
+        P->jobs.assign(jobs, jobs + njobs);
+        for (int k = 0; k < njobs; ++k) check_job(jobs[k], k);
+        const TileCfg tc = tile_cfg(c.opt.kernel);
+        P->phase1 = std::make_unique<Batch>(c, tc);
+        P->phase3 = std::make_unique<Batch>(c, tc);
+        P->fwd_true.assign(njobs, nullptr);
+        P->fwd_bg.assign(njobs, nullptr);
+        P->adj.assign(njobs, nullptr);
+        for (int k = 0; k < njobs; ++k) {
+            const mnad_job& j = jobs[k];
+            P->fwd_true[k] = add_prop(*P, j, MODE_FWD, j.v, nullptr, 0);
+            if (j.kind == MNAD_JOB_RTM) {
+                double vmin, vmax;
+                model_minmax(j.vs, (size_t)j.nz * j.nx, vmin, vmax);
+                const int nf = snapshot_nf(j.nt, vmin, vmax);
+                const int T = j.T > 0 ? j.T : snapshot_T(j.nt, nf);
+                const int ks = j.nt / T;
+                P->wfs.push_back(new_wavefield(c, j.nz, j.nx, j.d_pml, j.nt, T, std::max(2 * nf + 1, ks), ks,
+                                               c.opt.snapshot_codec));
+                Wavefield* wf = P->wfs.back().get();
+                P->fwd_bg[k] = add_prop(*P, j, MODE_FWD, j.vs, wf, T);
+                P->adj[k] = add_prop(*P, j, MODE_ADJ, j.vs, wf, T);
+            }
+        }
+        for (auto& p : P->props) {
+            p->build(c, tc);
+            (p->spec.mode == MODE_FWD ? P->phase1 : P->phase3)->add(p.get());
+            P->pts += p->point_updates();
+            P->bytes += p->algorithmic_bytes();
+        }
+        P->phase1->finalize();
+        P->phase3->finalize();
+        for (auto& e : P->ev) MNAD_CK(cudaEventCreate(&e));
+        c.sync();
+        *out = P.release();
+    });
+}
+
+MNAD_API int mnad_plan_run(mnad_plan* P)
+{
+    return guard([&] {
+        need(P != nullptr, "plan is NULL");
+        Context& c = *P->ctx;
+        MNAD_CK(cudaSetDevice(c.device));
+        const bool g = c.opt.use_graphs != 0;
+        MNAD_CK(cudaEventRecord(P->ev[0], c.stream));
+        P->phase1->run(g);
+        MNAD_CK(cudaEventRecord(P->ev[1], c.stream));
+        for (size_t k = 0; k < P->jobs.size(); ++k) {
+            if (!P->adj[k]) continue;
+            const size_t n = (size_t)P->jobs[k].nt * P->jobs[k].nr;
+            if (n == 0) continue;
+            residual_f64<<<(int)std::min<size_t>((n + 255) / 256, 1024), 256, 0, c.stream>>>(
+                P->fwd_true[k]->data.as<double>(), P->fwd_bg[k]->data.as<double>(), n, P->adj[k]->data.as<double>());
+            MNAD_CK(cudaGetLastError());
+        }
+        MNAD_CK(cudaEventRecord(P->ev[2], c.stream));
+        P->phase3->run(g);
+        MNAD_CK(cudaEventRecord(P->ev[3], c.stream));
+        MNAD_CK(cudaEventSynchronize(P->ev[3]));
+        float a = 0, b = 0, t = 0;
+        MNAD_CK(cudaEventElapsedTime(&t, P->ev[0], P->ev[3]));
+        MNAD_CK(cudaEventElapsedTime(&a, P->ev[0], P->ev[1]));
+        MNAD_CK(cudaEventElapsedTime(&b, P->ev[2], P->ev[3]));
+        P->run_ms = t;
+        P->step_ms = a + b;
+        P->launches = P->phase1->steps() + P->phase3->steps();
+    });
+}
+
+MNAD_API int mnad_plan_download(mnad_plan* P)
+{
+    return guard([&] {
+        need(P != nullptr, "plan is NULL");
+        Context& c = *P->ctx;
+        MNAD_CK(cudaSetDevice(c.device));
+        std::vector<DevMem> tmp;
+        for (size_t k = 0; k < P->jobs.size(); ++k) {
+            const mnad_job& j = P->jobs[k];
+            const size_t nd = (size_t)j.nt * j.nr;
+            if (j.kind == MNAD_JOB_MODEL) {
+                if (nd) download(c, j.data_out, P->fwd_true[k]->data.get(), nd * sizeof(double));
+                continue;
+            }
+            Prop* a = P->adj[k];
+            if (j.data_out && nd) download(c, j.data_out, a->data.get(), nd * sizeof(double));
+            const size_t n = a->nint();
+            const int T = a->spec.T;
+            tmp.emplace_back(&c, n * sizeof(double));
+            scale_f64<<<(int)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c.stream>>>(
+                a->image.as<double>(), (double)T, n, tmp.back().as<double>());
+            MNAD_CK(cudaGetLastError());
+            download(c, j.image_out, tmp.back().get(), n * sizeof(double));
+            if (j.illum_out) {
+                tmp.emplace_back(&c, n * sizeof(double));
+                scale_f64<<<(int)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c.stream>>>(
+                    a->spec.wf->illum.as<double>(), (double)T, n, tmp.back().as<double>());
+                MNAD_CK(cudaGetLastError());
+                download(c, j.illum_out, tmp.back().get(), n * sizeof(double));
+            }
+        }
+        c.sync();
+    });
+}
+
+MNAD_API int mnad_plan_destroy(mnad_plan* P)
+{
+    return guard([&] {
+        if (P) MNAD_CK(cudaSetDevice(P->ctx->device));
+        delete P;
+    });
+}
+
+MNAD_API int mnad_plan_work(const mnad_plan* P, double* pts, double* bytes)
+{
+    return guard([&] {
+        need(P != nullptr, "plan is NULL");
+        if (pts) *pts = P->pts;
+        if (bytes) *bytes = P->bytes;
+    });
+}
+
+MNAD_API int mnad_plan_timing(const mnad_plan* P, double* run_ms, double* step_ms, int* launches)
+{
+    return guard([&] {
+        need(P != nullptr, "plan is NULL");
+        if (run_ms) *run_ms = P->run_ms;
+        if (step_ms) *step_ms = P->step_ms;
+        if (launches) *launches = P->launches;
+    });
+}
+
+MNAD_API int mnad_run_jobs(mnad_context* ctx, const mnad_job* jobs, int njobs)
+{
+    mnad_plan* P = nullptr;
+    int rc = mnad_plan_create(ctx, jobs, njobs, &P);
+    if (rc != MNAD_OK) return rc;
+    rc = mnad_plan_run(P);
+    if (rc == MNAD_OK) rc = mnad_plan_download(P);
+    const std::string keep = g_err;
+    const int rc2 = mnad_plan_destroy(P);
+    if (rc != MNAD_OK) {
+        g_err = keep;
+        return rc;
+    }
+    return rc2;
+}
+
+}  // extern "C"

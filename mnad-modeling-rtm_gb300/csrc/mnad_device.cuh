@@ -1,0 +1,187 @@
+// Device-side definitions shared by the MNAD step kernels.
+//
+// A "propagation" is one shot advancing one wavefield triple (U, V, W) in
+// time, forward (fwd_PDE_exact_MNAD.m) or reverse (Born_adj_MNAD.m).  Many
+// propagations (shots, possibly on different grids) advance together in one
+// launch per time step; each launch covers a flat list of tiles and every
+// tile knows its propagation through `tile_prop`.
+//
+// Storage of every per-point field (U, V, W, both time levels, and r=v^2dt^2)
+// is column-major with z fastest, exactly like the MATLAB arrays, with a
+// zero halo: element (j, i) lives at base[(i + HX) * ld + (j + HZ)].  The halo
+// is never written, so it reproduces the reference's omission of out-of-grid
+// neighbours (the index ranges in SRC/MNAD/A??_gen.m) without bounds checks,
+// and every 2-D tile including its halo is in-bounds for TMA.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace mnad {
+
+constexpr int HZ = 4;   // zero rows before row 0 (keeps column starts 16-byte aligned)
+constexpr int HZB = 4;  // at least this many zero rows after row nz-1
+constexpr int HX = 2;   // zero columns on each side (V needs x +- 2)
+
+enum Mode { MODE_FWD = 0, MODE_ADJ = 1 };
+enum Codec { CODEC_F32 = 0, CODEC_BF16 = 1, CODEC_F16 = 2 };
+enum Pairing { PAIR_REFERENCE = 0, PAIR_ALIGNED = 1 };
+
+// Status bits written by kernels (never traps).
+enum StatusBits : unsigned {
+    ST_NONFINITE = 1u,     // a non-finite value was produced
+    ST_F16_RANGE = 2u,     // an FP16 snapshot value saturated
+};
+
+// The 24 distinct stencil coefficients of one destination point.  Each is
+// alpha*r + beta*r^2 with r = v^2 dt^2 at the destination (the reference's
+// v(j,i).^2*dt^2 and v(j,i).^4*dt^4 terms); for the three centre entries the
+// constant 2 is kept out and added exactly in the update.  The sign pattern
+// of the odd couplings is applied in mnad_update().
+enum Coef {
+    K_UU_Z, K_UU_X, K_UU_C, K_UU_D,          // Auu_gen.m
+    K_UV_X1, K_UV_D, K_UV_X2,                // Auv_gen.m
+    K_UW_Z1, K_UW_D, K_UW_Z2,                // Auw_gen.m
+    K_VU_X1, K_VU_D,                         // Avu_gen.m
+    K_VV_Z, K_VV_X, K_VV_C, K_VV_D,          // Avv_gen.m
+    K_VW,                                    // Avw_gen.m
+    K_WU_Z1, K_WU_D,                         // Awu_gen.m
+    K_WV,                                    // Awv_gen.m
+    K_WW_Z, K_WW_X, K_WW_C, K_WW_D,          // Aww_gen.m
+    NCOEF
+};
+
+struct PropDesc {
+    int mode;          // MODE_FWD / MODE_ADJ
+    int nt;            // steps of this propagation
+    int nz, nx;        // padded grid (as passed to the reference)
+    int ld;            // z pitch of per-point storage (floats)
+    int d;             // CPML thickness (d_pml)
+    int dpz;           // pitch of one z-strip column (floats, >= d)
+    int tile_base;     // first global tile of this propagation
+    int ntz, ntx;      // tiles along z / x
+    float* fld[2][3];  // [time level][U,V,W], storage origin (halo included)
+    const float* r;    // v^2 dt^2, same storage
+    float* mx;         // x-strip memory variables [side 2][var 9][d][ld]
+    float* mz;         // z-strip memory variables [side 2][var 9][nx][dpz]
+    float kx, kz;      // 3 ln(1/R) / (2 D^3), D = d*dx or d*dz (C_cof.m:6,38)
+    float dx, dz, dt, inv_dt;
+    float alpha[NCOEF], beta[NCOEF];
+    // source (forward): storage offset of the point and the amount
+    // r_src*w(tt) injected at each step (fwd_PDE_exact_MNAD.m:111)
+    int src;                 // -1: none
+    const float* src_amp;    // [nt]
+    // receivers, bucketed per tile: entries tile_rec[t]..tile_rec[t+1]
+    int nr;
+    const int* rec_pt;       // storage offset of each entry
+    const int* rec_id;       // receiver column rr of each entry
+    const double* rec_r;     // r at the receiver (adjoint injection scale)
+    const int* tile_rec;     // [ntz*ntx + 1]
+    double* data;            // [nr][nt] (column-major nt x nr): fwd out / adj in
+    double* datav;           // optional fwd outputs
+    double* dataw;
+    // snapshots (forward with indx==1) / imaging (adjoint)
+    int T;                   // 0: none
+    int nsnap;               // snapshots filled by the forward: floor(nt/T)
+    int ncols;               // columns of the reference's UU matrix
+    int codec;
+    int pairing;
+    int img_steps;           // adjoint: number of imaging steps floor(nt/T)
+    void* snap;              // [ncols' = nsnap][nint]
+    const float* snap_scale; // per-snapshot scale (FP16 codec), may be null
+    double* illum;           // [nint] sum of d2u^2 (forward)
+    double* image;           // [nint] sum of US.*UR (adjoint)
+    float inv_dt2;
+    unsigned* status;
+};
+
+__device__ __forceinline__ float coef(const PropDesc& P, int k, float r, float q)
+{
+    return fmaf(P.beta[k], q, P.alpha[k] * r);
+}
+
+// Neighbourhood of one point for the three fields.  Naming: <f><z><x> with
+// z/x in {m: -1, 0: 0, p: +1}; the x+-2 (V) and z+-2 (W) reaches are extra.
+struct Hood {
+    float u00, uzm, uzp, uxm, uxp, umm, upm, ump, upp;
+    float v00, vzm, vzp, vxm, vxp, vmm, vpm, vmp, vpp, vxm2, vxp2;
+    float w00, wzm, wzp, wxm, wxp, wmm, wpm, wmp, wpp, wzm2, wzp2;
+};
+
+// Sigma_G A_FG * G without the exact "2*F" centre part, for F = U, V, W
+// (fwd_PDE_exact_MNAD.m:114-116).  Coefficient signs: the odd couplings use
+// one coefficient with the sign taken from the J index arrays of the
+// generator files (e.g. Auv_gen.m:119-170: +c at i+1, -c at i-1, +c at i-2).
+__device__ __forceinline__ void mnad_update(const PropDesc& P, float r, const Hood& h,
+                                            float& su, float& sv, float& sw)
+{
+    const float q = r * r;
+    // nU row
+    float a = coef(P, K_UU_C, r, q) * h.u00;
+    a = fmaf(coef(P, K_UU_Z, r, q), h.uzm + h.uzp, a);
+    a = fmaf(coef(P, K_UU_X, r, q), h.uxm + h.uxp, a);
+    a = fmaf(P.beta[K_UU_D] * q, (h.umm + h.upp) + (h.upm + h.ump), a);
+    a = fmaf(coef(P, K_UV_X1, r, q), h.vxp - h.vxm, a);
+    a = fmaf(P.beta[K_UV_D] * q, (h.vmp + h.vpp) - (h.vmm + h.vpm), a);
+    a = fmaf(coef(P, K_UV_X2, r, q), h.vxm2 - h.vxp2, a);
+    a = fmaf(coef(P, K_UW_Z1, r, q), h.wzp - h.wzm, a);
+    a = fmaf(P.beta[K_UW_D] * q, (h.wpm + h.wpp) - (h.wmm + h.wmp), a);
+    a = fmaf(coef(P, K_UW_Z2, r, q), h.wzm2 - h.wzp2, a);
+    su = a;
+    // nV row
+    float b = coef(P, K_VV_C, r, q) * h.v00;
+    b = fmaf(coef(P, K_VV_Z, r, q), h.vzm + h.vzp, b);
+    b = fmaf(coef(P, K_VV_X, r, q), h.vxm + h.vxp, b);
+    b = fmaf(P.beta[K_VV_D] * q, (h.vmm + h.vpp) + (h.vpm + h.vmp), b);
+    b = fmaf(coef(P, K_VU_X1, r, q), h.uxm - h.uxp, b);
+    b = fmaf(coef(P, K_VU_D, r, q), (h.umm + h.upm) - (h.ump + h.upp), b);
+    b = fmaf(coef(P, K_VW, r, q), (h.wmm + h.wpp) - (h.wpm + h.wmp), b);
+    sv = b;
+    // nW row
+    float c = coef(P, K_WW_C, r, q) * h.w00;
+    c = fmaf(coef(P, K_WW_Z, r, q), h.wzm + h.wzp, c);
+    c = fmaf(coef(P, K_WW_X, r, q), h.wxm + h.wxp, c);
+    c = fmaf(P.beta[K_WW_D] * q, (h.wmm + h.wpp) + (h.wpm + h.wmp), c);
+    c = fmaf(coef(P, K_WU_Z1, r, q), h.uzm - h.uzp, c);
+    c = fmaf(coef(P, K_WU_D, r, q), (h.umm + h.ump) - (h.upm + h.upp), c);
+    c = fmaf(coef(P, K_WV, r, q), (h.vmm + h.vpp) - (h.vpm + h.vmp), c);
+    sw = c;
+}
+
+// CPML coefficients of C_cof.m:6-16 at one strip point.  X is the distance
+// term of x_b/z_b (D, D-h, ..., h on the low side; h, ..., D on the high side).
+__device__ __forceinline__ void cpml_coefs(float K, float v, float X, float dt,
+                                           float& c1, float& c2, float& c3)
+{
+    const float s0 = K * v;
+    const float sig = s0 * (X * X);
+    const float dsig = 2.0f * s0 * X;
+    const float inv_den = 1.0f / fmaf(sig, 0.5f * dt, 1.0f);
+    c1 = (1.0f - sig * (0.5f * dt)) * inv_den;
+    c2 = (dsig * dt) * inv_den;
+    c3 = (sig * dt) * inv_den;
+}
+
+// One side of Ux123_gen.m / Uz123_gen.m for one field at one point:
+// gr = (behind - ahead) on the low side, (ahead - behind) on the high side;
+// lap = behind - 2 F + ahead.  Updates m1..m3 in place, returns the new m1.
+__device__ __forceinline__ float cpml_mem(float c1, float c2, float c3, float inv_h,
+                                          float gr, float lap, float& m1, float& m2, float& m3)
+{
+    const float inv_h2 = inv_h * inv_h;
+    const float g2 = c2 * inv_h * gr;                 // (c2/h)*gr
+    m3 = fmaf(c1, m3, 0.5f * g2);
+    m2 = fmaf(c1, m2, g2) + c3 * fmaf(lap, inv_h2, -m3);
+    m1 = fmaf(c1, m1, 0.5f * g2) + c3 * fmaf(2.0f * lap, inv_h2, -m2);
+    return m1;
+}
+
+__device__ __forceinline__ float snap_decode(const void* base, int codec, size_t i, float scale)
+{
+    if (codec == CODEC_BF16) return __bfloat162float(static_cast<const __nv_bfloat16*>(base)[i]);
+    if (codec == CODEC_F16) return __half2float(static_cast<const __half*>(base)[i]) * scale;
+    return static_cast<const float*>(base)[i];
+}
+
+}  // namespace mnad

@@ -1,0 +1,405 @@
+// Host-side engine: device memory, propagation setup, batched time loop.
+#include "mnad_engine.h"
+#include "mnad_kernels.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace mnad {
+
+void check_cuda(cudaError_t e, const char* what, const char* file, int line)
+{
+    if (e == cudaSuccess) return;
+    const int code = (e == cudaErrorMemoryAllocation) ? MNAD_E_OOM : MNAD_E_CUDA;
+    throw Error(code, std::string(cudaGetErrorString(e)) + " in " + what + " (" + file + ":" + std::to_string(line) + ")");
+}
+
+static size_t round_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
+
+// ---------------------------------------------------------------------------
+DevMem::DevMem(Context* c, size_t bytes) : ctx_(c), n_(bytes)
+{
+    p_ = bytes ? c->alloc(bytes) : nullptr;
+}
+
+DevMem& DevMem::operator=(DevMem&& o) noexcept
+{
+    if (this != &o) {
+        reset();
+        ctx_ = o.ctx_; p_ = o.p_; n_ = o.n_;
+        o.ctx_ = nullptr; o.p_ = nullptr; o.n_ = 0;
+    }
+    return *this;
+}
+
+void DevMem::reset()
+{
+    if (p_ && ctx_) ctx_->release(p_, n_);
+    p_ = nullptr; n_ = 0; ctx_ = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+Context::Context(int dev, size_t budget_bytes) : device(dev), budget(budget_bytes)
+{
+    MNAD_CK(cudaSetDevice(dev));
+    MNAD_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    MNAD_CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
+    cudaMemPool_t pool;
+    MNAD_CK(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t keep = UINT64_MAX;   // keep freed blocks cached for the next job
+    MNAD_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    MNAD_CK(cudaMalloc(&d_status, sizeof(unsigned)));
+    MNAD_CK(cudaMemset(d_status, 0, sizeof(unsigned)));
+    opt.snapshot_codec = MNAD_SNAP_F32;
+    opt.pairing = MNAD_PAIR_REFERENCE;
+    opt.T = 0;
+    opt.record_vw = 0;
+    opt.use_graphs = 1;
+    opt.kernel = MNAD_KERNEL_AUTO;
+}
+
+Context::~Context()
+{
+    if (stream) cudaStreamSynchronize(stream);
+    wavefields.clear();
+    if (d_status) cudaFree(d_status);
+    if (stream) cudaStreamSynchronize(stream), cudaStreamDestroy(stream);
+}
+
+void* Context::alloc(size_t bytes)
+{
+    if (budget && in_use + bytes > budget)
+        throw Error(MNAD_E_BUDGET, "allocation of " + std::to_string(bytes) + " B exceeds the context budget (" +
+                                       std::to_string(in_use) + " of " + std::to_string(budget) + " B in use)");
+    void* p = nullptr;
+    MNAD_CK(cudaMallocAsync(&p, bytes, stream));
+    in_use += bytes;
+    return p;
+}
+
+void Context::release(void* p, size_t bytes)
+{
+    cudaFreeAsync(p, stream);
+    in_use -= std::min(in_use, bytes);
+}
+
+void Context::sync() { MNAD_CK(cudaStreamSynchronize(stream)); }
+
+unsigned Context::take_status()
+{
+    unsigned s = 0;
+    MNAD_CK(cudaMemcpyAsync(&s, d_status, sizeof(s), cudaMemcpyDeviceToHost, stream));
+    MNAD_CK(cudaMemsetAsync(d_status, 0, sizeof(unsigned), stream));
+    sync();
+    return s;
+}
+
+void upload(Context& ctx, void* dst, const void* src, size_t bytes)
+{
+    if (bytes) MNAD_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx.stream));
+    ctx.h2d += bytes;
+}
+
+void download(Context& ctx, void* dst, const void* src, size_t bytes)
+{
+    if (bytes) MNAD_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.d2h += bytes;
+}
+
+// ---------------------------------------------------------------------------
+TileCfg tile_cfg(int kernel)
+{
+    (void)kernel;
+    return TileCfg{MNAD_KERNEL_DIRECT, DIRECT_TZ, DIRECT_TX};
+}
+
+void model_minmax(const double* v, size_t n, double& vmin, double& vmax)
+{
+    vmin = INFINITY; vmax = -INFINITY;
+    for (size_t k = 0; k < n; ++k) {
+        vmin = std::min(vmin, v[k]);
+        vmax = std::max(vmax, v[k]);
+    }
+}
+
+int snapshot_nf(int nt, double vmin, double vmax)
+{
+    // nf = floor(nt/(2*3*max(v(:))/min(v(:)))), same evaluation order.
+    return (int)std::floor((double)nt / (2.0 * 3.0 * vmax / vmin));
+}
+
+int snapshot_T(int nt, int nf)
+{
+    if (nf <= 0)
+        throw Error(MNAD_E_ARG, "snapshot plan: nf = floor(nt/(6*vmax/vmin)) is 0, so T = floor(nt/nf/2) is "
+                                "undefined; set mnad_options.T");
+    return (int)std::floor((double)nt / nf / 2.0);
+}
+
+// Stencil coefficient polynomials alpha*r + beta*r^2 (r = v^2 dt^2) of the
+// nine generator files, centre entries without their constant 2.
+static void stencil_polys(double dx, double dz, float* al, float* be)
+{
+    const double dx2 = dx * dx, dz2 = dz * dz, dx3 = dx2 * dx, dz3 = dz2 * dz;
+    const double dx4 = dx2 * dx2, dz4 = dz2 * dz2, dx5 = dx4 * dx, dz5 = dz4 * dz;
+    double a[NCOEF] = {}, b[NCOEF] = {};
+    // Auu_gen.m:30,37,44,65
+    a[K_UU_Z] = (24.0 / 11) / dz2;   b[K_UU_Z] = -(15 / (11 * dz4) + 1 / (dx2 * dz2));
+    a[K_UU_X] = (24.0 / 11) / dx2;   b[K_UU_X] = -(15 / (11 * dx4) + 1 / (dx2 * dz2));
+    a[K_UU_C] = -(48.0 / 11) * (1 / dx2 + 1 / dz2);
+    b[K_UU_C] = (30.0 / 11) * (1 / dx4 + 1 / dz4 + 11 / (15 * dx2 * dz2));
+    b[K_UU_D] = 1 / (2 * dx2 * dz2);
+    // Auv_gen.m:128 (i+1), 149 (diagonals at i+1), 163 (i-2)
+    a[K_UV_X1] = (20.0 / 33) / dx;   b[K_UV_X1] = -(47 / (66 * dx3) + 1 / (6 * dx * dz2));
+    b[K_UV_D] = 1 / (12 * dx * dz2);
+    a[K_UV_X2] = (1.0 / 132) / dx;   b[K_UV_X2] = -(1.0 / 66) / dx3;
+    // Auw_gen.m:205 (j+1), 226 (diagonals at j+1), 254 (j-2)
+    a[K_UW_Z1] = (20.0 / 33) / dz;   b[K_UW_Z1] = -(47 / (66 * dz3) + 1 / (6 * dz * dx2));
+    b[K_UW_D] = 1 / (12 * dz * dx2);
+    a[K_UW_Z2] = (1.0 / 132) / dz;   b[K_UW_Z2] = -(1.0 / 66) / dz3;
+    // Avu_gen.m:30 (i-1), 44 (diagonals at i-1)
+    a[K_VU_X1] = 15 / (2 * dx3) - 1 / (dx * dz2);
+    b[K_VU_X1] = -(15 / (2 * dx5) - 1 / (dx * dz4) + 5 / (2 * dx3 * dz2));
+    a[K_VU_D] = 1 / (2 * dx * dz2);  b[K_VU_D] = 5 / (4 * dx3 * dz2) - 1 / (2 * dx * dz4);
+    // Avv_gen.m:101,108,115,136
+    a[K_VV_Z] = 1 / dz2;             b[K_VV_Z] = -2 / (dx2 * dz2);
+    a[K_VV_X] = -1.5 / dx2;          b[K_VV_X] = 5 / (2 * dx4) + 1 / (2 * dx2 * dz2);
+    a[K_VV_C] = -(12 / dx2 + 2 / dz2); b[K_VV_C] = 10 / dx4 + 4 / (dx2 * dz2);
+    b[K_VV_D] = -1 / (4 * dx2 * dz2);
+    // Avw_gen.m:192 ((j-1,i-1) and (j+1,i+1))
+    a[K_VW] = -1 / (4 * dz * dx);    b[K_VW] = 1 / (4 * dz3 * dx);
+    // Awu_gen.m:29 (j-1), 44 (diagonals at j-1)
+    a[K_WU_Z1] = 15 / (2 * dz3) - 1 / (dz * dx2);
+    b[K_WU_Z1] = -(15 / (2 * dz5) - 1 / (dz * dx4) + 5 / (2 * dz3 * dx2));
+    a[K_WU_D] = 1 / (2 * dz * dx2);  b[K_WU_D] = 5 / (4 * dz3 * dx2) - 1 / (2 * dz * dx4);
+    // Awv_gen.m:106 ((j-1,i-1) and (j+1,i+1))
+    a[K_WV] = -1 / (4 * dz * dx);    b[K_WV] = 1 / (4 * dx3 * dz);
+    // Aww_gen.m:164,171,178,199
+    a[K_WW_Z] = -1.5 / dz2;          b[K_WW_Z] = 5 / (2 * dz4) + 1 / (2 * dx2 * dz2);
+    a[K_WW_X] = 1 / dx2;             b[K_WW_X] = -2 / (dz2 * dx2);
+    a[K_WW_C] = -(12 / dz2 + 2 / dx2); b[K_WW_C] = 10 / dz4 + 4 / (dx2 * dz2);
+    b[K_WW_D] = -1 / (4 * dx2 * dz2);
+    for (int k = 0; k < NCOEF; ++k) { al[k] = (float)a[k]; be[k] = (float)b[k]; }
+}
+
+static double r_of(double v, double dt, int mode)
+{
+    return mode == MODE_ADJ ? (v * dt) * (v * dt) : (v * v) * (dt * dt);
+}
+
+// ---------------------------------------------------------------------------
+void Prop::build(Context& ctx, const TileCfg& tc)
+{
+    const PropSpec& s = spec;
+    const int nz = s.nz, nx = s.nx, d = s.d;
+    const int ld = (int)round_up((size_t)nz + HZ + HZB, 32);
+    S = (size_t)ld * (nx + 2 * HX);
+    const int dpz = (int)round_up((size_t)std::max(d, 1), 4);
+    cudaStream_t st = ctx.stream;
+
+    fields = DevMem(&ctx, 6 * S * sizeof(float));
+    r = DevMem(&ctx, S * sizeof(float));
+    MNAD_CK(cudaMemsetAsync(r.get(), 0, r.size(), st));
+    if (d > 0) {
+        mx = DevMem(&ctx, (size_t)2 * 9 * d * ld * sizeof(float));
+        mz = DevMem(&ctx, (size_t)2 * 9 * nx * dpz * sizeof(float));
+    }
+    const size_t N = (size_t)nz * nx;
+    {
+        DevMem vt(&ctx, N * sizeof(double));
+        upload(ctx, vt.get(), s.v, N * sizeof(double));
+        const int blocks = (int)std::min<size_t>((N + 255) / 256, (size_t)ctx.num_sms * 8);
+        build_r<<<blocks, 256, 0, st>>>(vt.as<double>(), nz, nx, s.dt, s.mode == MODE_ADJ, r.as<float>(), ld);
+        MNAD_CK(cudaGetLastError());
+    }
+
+    PropDesc& D = desc;
+    std::memset(&D, 0, sizeof(D));
+    D.mode = s.mode; D.nt = s.nt; D.nz = nz; D.nx = nx; D.ld = ld; D.d = d; D.dpz = dpz;
+    D.ntz = (nz + tc.tz - 1) / tc.tz;
+    D.ntx = (nx + tc.tx - 1) / tc.tx;
+    for (int t = 0; t < 2; ++t)
+        for (int f = 0; f < 3; ++f) D.fld[t][f] = fields.as<float>() + (size_t)(t * 3 + f) * S;
+    D.r = r.as<float>();
+    D.mx = mx.as<float>();
+    D.mz = mz.as<float>();
+    const double R = 1e-4;   // fwd_PDE_exact_MNAD.m:88
+    if (d > 0) {
+        D.kx = (float)((3 * std::log(1 / R)) / (2 * std::pow(d * s.dx, 3)));
+        D.kz = (float)((3 * std::log(1 / R)) / (2 * std::pow(d * s.dz, 3)));
+    }
+    D.dx = (float)s.dx; D.dz = (float)s.dz; D.dt = (float)s.dt; D.inv_dt = (float)(1.0 / s.dt);
+    D.inv_dt2 = (float)(1.0 / (s.dt * s.dt));
+    stencil_polys(s.dx, s.dz, D.alpha, D.beta);
+    D.status = ctx.d_status;
+
+    auto off = [&](int j, int i) { return (int)((size_t)(i + HX) * ld + (j + HZ)); };
+    D.src = -1;
+    if (s.mode == MODE_FWD && s.zs >= 0) {
+        D.src = off(s.zs, s.xs);
+        std::vector<float> amp(s.nt);
+        const double rs = r_of(s.v[(size_t)s.zs + (size_t)s.xs * nz], s.dt, MODE_FWD);
+        for (int t = 0; t < s.nt; ++t) amp[t] = (float)(rs * s.w[t]);     // fwd_PDE_exact_MNAD.m:111
+        src_amp = DevMem(&ctx, s.nt * sizeof(float));
+        upload(ctx, src_amp.get(), amp.data(), amp.size() * sizeof(float));
+        D.src_amp = src_amp.as<float>();
+    }
+
+    // Receivers bucketed by tile (counting sort).
+    const int nr = (int)s.zr.size();
+    const int ntiles = D.ntz * D.ntx;
+    std::vector<int> cnt(ntiles + 1, 0), pt(nr), id(nr);
+    std::vector<double> rr(nr);
+    for (int k = 0; k < nr; ++k) cnt[1 + (s.zr[k] / tc.tz) + (s.xr[k] / tc.tx) * D.ntz]++;
+    for (int t = 0; t < ntiles; ++t) cnt[t + 1] += cnt[t];
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int k = 0; k < nr; ++k) {
+        const int t = (s.zr[k] / tc.tz) + (s.xr[k] / tc.tx) * D.ntz;
+        const int e = fill[t]++;
+        pt[e] = off(s.zr[k], s.xr[k]);
+        id[e] = k;
+        rr[e] = r_of(s.v[(size_t)s.zr[k] + (size_t)s.xr[k] * nz], s.dt, s.mode);
+    }
+    D.nr = nr;
+    tile_rec = DevMem(&ctx, (ntiles + 1) * sizeof(int));
+    upload(ctx, tile_rec.get(), cnt.data(), (ntiles + 1) * sizeof(int));
+    D.tile_rec = tile_rec.as<int>();
+    if (nr > 0) {
+        rec_pt = DevMem(&ctx, nr * sizeof(int));
+        rec_id = DevMem(&ctx, nr * sizeof(int));
+        rec_r = DevMem(&ctx, nr * sizeof(double));
+        upload(ctx, rec_pt.get(), pt.data(), nr * sizeof(int));
+        upload(ctx, rec_id.get(), id.data(), nr * sizeof(int));
+        upload(ctx, rec_r.get(), rr.data(), nr * sizeof(double));
+        data = DevMem(&ctx, (size_t)nr * s.nt * sizeof(double));
+        if (s.mode == MODE_FWD && s.record_vw) {
+            datav = DevMem(&ctx, (size_t)nr * s.nt * sizeof(double));
+            dataw = DevMem(&ctx, (size_t)nr * s.nt * sizeof(double));
+        }
+    }
+    D.rec_pt = rec_pt.as<int>(); D.rec_id = rec_id.as<int>(); D.rec_r = rec_r.as<double>();
+    D.data = data.as<double>(); D.datav = datav.as<double>(); D.dataw = dataw.as<double>();
+
+    if (s.T > 0 && s.wf) {
+        Wavefield& wf = *s.wf;
+        D.T = s.T;
+        D.nsnap = wf.nsnap;
+        D.ncols = wf.ncols;
+        D.codec = wf.codec;
+        D.pairing = s.pairing;
+        D.snap = wf.snap.get();
+        D.snap_scale = wf.scale.as<float>();
+        if (s.mode == MODE_FWD) {
+            D.illum = wf.illum.as<double>();
+        } else {
+            D.img_steps = s.nt / s.T;
+            image = DevMem(&ctx, nint() * sizeof(double));
+            D.image = image.as<double>();
+        }
+    }
+}
+
+void Prop::reset(Context& ctx)
+{
+    cudaStream_t st = ctx.stream;
+    MNAD_CK(cudaMemsetAsync(fields.get(), 0, fields.size(), st));
+    if (mx.get()) MNAD_CK(cudaMemsetAsync(mx.get(), 0, mx.size(), st));
+    if (mz.get()) MNAD_CK(cudaMemsetAsync(mz.get(), 0, mz.size(), st));
+    if (spec.mode == MODE_FWD) {
+        if (data.get()) MNAD_CK(cudaMemsetAsync(data.get(), 0, data.size(), st));
+        if (desc.illum) MNAD_CK(cudaMemsetAsync(desc.illum, 0, nint() * sizeof(double), st));
+    } else if (image.get()) {
+        MNAD_CK(cudaMemsetAsync(image.get(), 0, image.size(), st));
+    }
+}
+
+double Prop::algorithmic_bytes() const
+{
+    // Per point-step: read U,V,W,pU,pV,pW,r and write nU,nV,nW (40 B FP32);
+    // per CPML strip point and direction: 9 memory variables read + written
+    // (72 B); snapshot steps: codec bytes + FP64 illumination r+w (forward)
+    // or codec bytes + FP64 image r+w (adjoint).
+    const double N = (double)spec.nz * spec.nx;
+    const double strip = spec.d > 0 ? 2.0 * spec.d * (spec.nz + spec.nx) : 0.0;
+    double b = (N * 40.0 + strip * 72.0) * spec.nt;
+    if (spec.T > 0 && spec.wf) {
+        const double cb = spec.wf->codec == MNAD_SNAP_F32 ? 4.0 : 2.0;
+        b += (double)nint() * (cb + 16.0) * (spec.nt / spec.T);
+    }
+    return b;
+}
+
+// ---------------------------------------------------------------------------
+Batch::~Batch()
+{
+    if (graph_) cudaGraphExecDestroy(graph_);
+}
+
+void Batch::finalize()
+{
+    std::vector<PropDesc> descs;
+    std::vector<int> tile_prop;
+    nsteps_ = 0;
+    for (size_t k = 0; k < props_.size(); ++k) {
+        PropDesc& D = props_[k]->desc;
+        D.tile_base = (int)tile_prop.size();
+        tile_prop.insert(tile_prop.end(), (size_t)D.ntz * D.ntx, (int)k);
+        descs.push_back(D);
+        nsteps_ = std::max(nsteps_, D.nt);
+    }
+    ntiles_ = (int)tile_prop.size();
+    d_desc_ = DevMem(&ctx_, std::max<size_t>(1, descs.size()) * sizeof(PropDesc));
+    d_tile_prop_ = DevMem(&ctx_, std::max<size_t>(1, tile_prop.size()) * sizeof(int));
+    upload(ctx_, d_desc_.get(), descs.data(), descs.size() * sizeof(PropDesc));
+    upload(ctx_, d_tile_prop_.get(), tile_prop.data(), tile_prop.size() * sizeof(int));
+}
+
+void Batch::launch_step(int s)
+{
+    dim3 block(DIRECT_TZ, DIRECT_TX);
+    step_direct<<<ntiles_, block, 0, ctx_.stream>>>(d_desc_.as<PropDesc>(), d_tile_prop_.as<int>(), s);
+}
+
+void Batch::start()
+{
+    for (Prop* p : props_) p->reset(ctx_);
+    if (!props_.empty())
+        seed_sources<<<((int)props_.size() + 127) / 128, 128, 0, ctx_.stream>>>(d_desc_.as<PropDesc>(), (int)props_.size());
+    MNAD_CK(cudaGetLastError());
+}
+
+void Batch::advance(int s0, int s1)
+{
+    if (ntiles_ == 0) return;
+    for (int s = s0; s < s1; ++s) launch_step(s);
+    MNAD_CK(cudaGetLastError());
+}
+
+void Batch::run(bool use_graph)
+{
+    if (ntiles_ == 0) return;
+    auto body = [&]() {
+        start();
+        advance(0, nsteps_);
+    };
+    if (!use_graph) {
+        body();
+        MNAD_CK(cudaGetLastError());
+        return;
+    }
+    if (!graph_) {
+        cudaGraph_t g = nullptr;
+        MNAD_CK(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal));
+        body();
+        cudaError_t e = cudaStreamEndCapture(ctx_.stream, &g);
+        MNAD_CK(e);
+        MNAD_CK(cudaGetLastError());
+        e = cudaGraphInstantiate(&graph_, g, 0);
+        cudaGraphDestroy(g);
+        MNAD_CK(e);
+    }
+    MNAD_CK(cudaGraphLaunch(graph_, ctx_.stream));
+}
+
+}  // namespace mnad

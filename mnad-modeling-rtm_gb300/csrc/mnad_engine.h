@@ -1,0 +1,144 @@
+// Host-side engine of the MNAD library: context, device memory, propagations,
+// batches and plans.  Internal; the public surface is include/mnad.h.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mnad.h"
+#include "mnad_device.cuh"
+
+namespace mnad {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void check_cuda(cudaError_t e, const char* what, const char* file, int line);
+#define MNAD_CK(x) ::mnad::check_cuda((x), #x, __FILE__, __LINE__)
+
+struct Context;
+
+// Stream-ordered device allocation owned by a context (RAII, move-only).
+class DevMem {
+public:
+    DevMem() = default;
+    DevMem(Context* c, size_t bytes);
+    ~DevMem() { reset(); }
+    DevMem(DevMem&& o) noexcept { *this = std::move(o); }
+    DevMem& operator=(DevMem&& o) noexcept;
+    DevMem(const DevMem&) = delete;
+    DevMem& operator=(const DevMem&) = delete;
+    void reset();
+    template <class T> T* as() const { return static_cast<T*>(p_); }
+    void* get() const { return p_; }
+    size_t size() const { return n_; }
+private:
+    Context* ctx_ = nullptr;
+    void* p_ = nullptr;
+    size_t n_ = 0;
+};
+
+// Source-side snapshots + illumination of one shot (the reference's
+// UU_<ss>.mat / illum_<ss>.mat pair), resident on the device.
+struct Wavefield {
+    int nz = 0, nx = 0, d = 0, nt = 0, T = 0, nsnap = 0, ncols = 0, codec = 0;
+    size_t nint = 0;
+    DevMem snap, scale, illum;
+};
+
+struct Context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    mnad_options opt{};
+    size_t budget = 0;        // 0: unbounded
+    size_t in_use = 0;
+    uint64_t h2d = 0, d2h = 0;   // bytes copied host->device / device->host
+    int num_sms = 0;
+    unsigned* d_status = nullptr;
+    std::map<int, std::unique_ptr<Wavefield>> wavefields;
+
+    explicit Context(int dev, size_t budget_bytes);
+    ~Context();
+    void* alloc(size_t bytes);
+    void release(void* p, size_t bytes);
+    void sync();
+    unsigned take_status();
+};
+
+// Tile shape of a step kernel; receivers are bucketed per tile of this shape.
+struct TileCfg {
+    int kind;   // MNAD_KERNEL_DIRECT / MNAD_KERNEL_TMA
+    int tz, tx;
+};
+TileCfg tile_cfg(int kernel);
+
+// Geometry and inputs of one propagation.
+struct PropSpec {
+    int mode = MODE_FWD;
+    int nz = 0, nx = 0, d = 0, nt = 0;
+    double dx = 0, dz = 0, dt = 0;
+    const double* v = nullptr;         // host model, nz*nx column-major
+    int zs = -1, xs = -1;              // 0-based source (forward), -1: none
+    const double* w = nullptr;         // host wavelet [nt]
+    std::vector<int> zr, xr;           // 0-based receivers
+    bool record_vw = false;
+    Wavefield* wf = nullptr;           // forward: snapshots to fill; adjoint: to image with
+    int T = 0;                         // snapshot / imaging interval (0: none)
+    int pairing = MNAD_PAIR_REFERENCE;
+};
+
+// Device state of one propagation.
+struct Prop {
+    PropSpec spec;
+    PropDesc desc{};
+    size_t S = 0;                      // floats per field in storage
+    DevMem fields, r, mx, mz, src_amp, rec_pt, rec_id, rec_r, tile_rec, data, datav, dataw, image;
+    void build(Context& ctx, const TileCfg& tc);
+    void reset(Context& ctx);          // zero the state of a fresh run (stream-ordered)
+    size_t nint() const { return (size_t)(spec.nz - 2 * spec.d) * (spec.nx - 2 * spec.d); }
+    double point_updates() const { return (double)spec.nz * spec.nx * spec.nt; }
+    double algorithmic_bytes() const;
+};
+
+// Propagations that advance together: one launch per time step.
+class Batch {
+public:
+    Batch(Context& ctx, const TileCfg& tc) : ctx_(ctx), tc_(tc) {}
+    ~Batch();
+    void add(Prop* p) { props_.push_back(p); }
+    void finalize();
+    void run(bool use_graph);          // start() + every step, optionally as one CUDA graph (async)
+    void start();                      // zero all state and seed the sources (async)
+    void advance(int s0, int s1);      // launch steps s0..s1-1 (async)
+    int steps() const { return nsteps_; }
+    int tiles() const { return ntiles_; }
+    const std::vector<Prop*>& props() const { return props_; }
+private:
+    void launch_step(int s);
+    Context& ctx_;
+    TileCfg tc_;
+    std::vector<Prop*> props_;
+    DevMem d_desc_, d_tile_prop_;
+    int ntiles_ = 0, nsteps_ = 0;
+    cudaGraphExec_t graph_ = nullptr;
+};
+
+// Model statistics for the reference's snapshot plan.
+void model_minmax(const double* v, size_t n, double& vmin, double& vmax);
+// nf of fwd_PDE_exact_MNAD.m:46 (may be 0).
+int snapshot_nf(int nt, double vmin, double vmax);
+// T of fwd_PDE_exact_MNAD.m:47 (throws when nf == 0).
+int snapshot_T(int nt, int nf);
+
+// Device copies of the shot records (FP64, nt x nr).
+void upload(Context& ctx, void* dst, const void* src, size_t bytes);
+void download(Context& ctx, void* dst, const void* src, size_t bytes);
+
+}  // namespace mnad

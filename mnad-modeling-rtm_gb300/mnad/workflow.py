@@ -1,0 +1,162 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+No dataset is involved: every model is generated here from a seed.  The
+drivers' conventions are kept: the physical model is padded by edge
+replication (``SRC/migration/main_Acoustic_RTM.m:148-149``), the Ricker
+wavelet is ``(1-2 tau^2) exp(-tau^2)``, ``tau = pi (t - 1.1/fc) fc``
+(``:138-140``), and grid indices are ``d_pml + metres/dx`` with
+``metres = dx * grid index`` (``:124-130`` with ``SRC/MNAD/acquisi.m:122-123,
+194``).  Receivers and sources are given as 1-based padded indices.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+
+def ricker(fc: float, dt: float, nt: int) -> np.ndarray:
+    t = np.arange(nt) * dt
+    tau = np.pi * (t - 1.1 / fc) * fc
+    return (1 - 2 * tau**2) * np.exp(-tau**2)
+
+
+def pad_model(V: np.ndarray, d: int) -> np.ndarray:
+    V = np.asarray(V, dtype=np.float64)
+    return np.pad(V, ((d, d), (d, d)), mode="edge")
+
+
+def gaussian_smooth(V: np.ndarray, taps: int, sigma: Optional[float] = None) -> np.ndarray:
+    """Separable Gaussian of ``taps`` points (sigma = taps/6 by default), edge-replicated."""
+    sigma = taps / 6.0 if sigma is None else sigma
+    h = taps // 2
+    k = np.exp(-0.5 * (np.arange(-h, h + 1) / sigma) ** 2)
+    k /= k.sum()
+    out = np.asarray(V, dtype=np.float64)
+    for ax in (0, 1):
+        p = np.pad(out, [(h, h) if a == ax else (0, 0) for a in (0, 1)], mode="edge")
+        acc = np.zeros_like(out)
+        for t in range(taps):
+            sl = [slice(None), slice(None)]
+            sl[ax] = slice(t, t + out.shape[ax])
+            acc += k[t] * p[tuple(sl)]
+        out = acc
+    return out
+
+
+@dataclass
+class Shot:
+    zs: int
+    xs: int
+    zr: np.ndarray
+    xr: np.ndarray
+
+
+@dataclass
+class Survey:
+    """A padded model (true and optionally migration), grid, time axis, shots."""
+    name: str
+    v: np.ndarray                     # padded true model (nz, nx)
+    dx: float
+    dz: float
+    dt: float
+    nt: int
+    d_pml: int
+    fc: float
+    shots: List[Shot]
+    vs: Optional[np.ndarray] = None   # padded migration model
+    T: int = 0                        # snapshot interval (0: reference formula)
+    codec: str = "f32"
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def w(self) -> np.ndarray:
+        return ricker(self.fc, self.dt, self.nt)
+
+    @property
+    def nz(self):
+        return self.v.shape[0]
+
+    @property
+    def nx(self):
+        return self.v.shape[1]
+
+
+def config1(nt: int = 1000) -> Survey:
+    """Plain FP64 forward modeling: 201 x 201 total grid (physical 161 x 161
+    plus a 20-point CPML), 10 m, 2000 m/s, 20 Hz Ricker at (101,101),
+    dt = 1 ms, 201 receivers on row 21 (the first physical row)."""
+    d = 20
+    v = np.full((201, 201), 2000.0)
+    shot = Shot(101, 101, np.full(201, 21), np.arange(1, 202))
+    return Survey("config1", v, 10.0, 10.0, 1e-3, nt, d, 20.0, [shot])
+
+
+def config2(seed: int = 0, nt: int = 3000, T: int = 4) -> Survey:
+    """Single-shot RTM: 301 (z) x 601 (x) at 10 m, layers 1500/2000/2600/3200
+    m/s with interfaces at 800/1600/2400 m, +300 m/s Gaussian anomaly
+    (sigma 150 m, centre from the seed); migration model = true model
+    smoothed by a 15-point Gaussian; 15 Hz; shot at x = 3000 m; 601
+    receivers at z = 20 m; dt = 1 ms; 3 s; snapshots every T = 4 steps."""
+    rng = np.random.default_rng(seed)
+    nzp, nxp, h, d = 301, 601, 10.0, 40
+    z = np.arange(nzp)[:, None] * h
+    x = np.arange(nxp)[None, :] * h
+    V = np.where(z < 800, 1500.0, np.where(z < 1600, 2000.0, np.where(z < 2400, 2600.0, 3200.0)))
+    V = np.broadcast_to(V, (nzp, nxp)).copy()
+    cz = rng.uniform(900, 2200)
+    cx = rng.uniform(1500, 4500)
+    V += 300.0 * np.exp(-((z - cz) ** 2 + (x - cx) ** 2) / (2 * 150.0**2))
+    Vs = gaussian_smooth(V, 15)
+    xs_grid, zs_grid, zr_grid = 300, 1, 2
+    shot = Shot(d + zs_grid, d + xs_grid, np.full(nxp, d + zr_grid), d + np.arange(1, nxp + 1))
+    return Survey("config2", pad_model(V, d), h, h, 1e-3, nt, d, 15.0, [shot], vs=pad_model(Vs, d), T=T,
+                  meta={"anomaly_centre_m": (cz, cx)})
+
+
+def gaussian_random_field(shape, h, corr, rng):
+    """Unit-variance field with a Gaussian covariance of correlation length ``corr`` (m)."""
+    nz, nx = shape
+    kz = np.fft.fftfreq(nz, d=h)[:, None]
+    kx = np.fft.fftfreq(nx, d=h)[None, :]
+    spec = np.exp(-((np.pi * corr) ** 2) * (kz**2 + kx**2) / 2)
+    f = np.real(np.fft.ifft2(np.fft.fft2(rng.standard_normal(shape)) * spec))
+    return (f - f.mean()) / (f.std() + 1e-30)
+
+
+def config3(seed: int = 0, nshots: int = 64, nt: int = 4000, codec: str = "bf16") -> Survey:
+    """Batched RTM: 401 (z) x 1201 (x) at 12.5 m; smooth Gaussian random field
+    (correlation 300 m) clipped to 1500-4000 m/s plus three dipping
+    +400 m/s reflectors; ``nshots`` shots every 187.5 m; 20 Hz; dt = 1 ms;
+    4 s; BF16 snapshots; migration model = 15-point Gaussian smoothing."""
+    rng = np.random.default_rng(seed)
+    nzp, nxp, h, d = 401, 1201, 12.5, 40
+    g = gaussian_random_field((nzp, nxp), h, 300.0, rng)
+    V = np.clip(2750.0 + 600.0 * g, 1500.0, 4000.0)
+    z = np.arange(nzp)[:, None] * h
+    x = np.arange(nxp)[None, :] * h
+    for _ in range(3):
+        z0 = rng.uniform(1200, 4200)
+        dip = np.tan(np.deg2rad(rng.uniform(-12, 12)))
+        band = np.abs(z - (z0 + dip * (x - x.mean()))) < 1.5 * h
+        V = V + 400.0 * band
+    Vs = gaussian_smooth(V, 15)
+    spacing = int(round(187.5 / h))
+    first = (nxp - spacing * (nshots - 1)) // 2
+    shots = []
+    for s in range(nshots):
+        xg = max(1, min(nxp, first + s * spacing))
+        shots.append(Shot(d + 1, d + xg, np.full(nxp, d + 2), d + np.arange(1, nxp + 1)))
+    return Survey("config3", pad_model(V, d), h, h, 1e-3, nt, d, 20.0, shots, vs=pad_model(Vs, d), codec=codec)
+
+
+def shot_jobs(sv: Survey, kind: str = "rtm", shots=None, keep_data: bool = False):
+    """mnad.api.ShotJob list for a survey (RTM: true + migration model)."""
+    from .api import ShotJob
+    out = []
+    for sh in (sv.shots if shots is None else shots):
+        out.append(ShotJob(kind=kind, v=sv.v, vs=sv.vs if kind == "rtm" else None, dx=sv.dx, dz=sv.dz, dt=sv.dt,
+                           nt=sv.nt, d_pml=sv.d_pml, zs=sh.zs, xs=sh.xs, zr=sh.zr, xr=sh.xr, w=sv.w, T=sv.T,
+                           keep_data=keep_data))
+    return out
