@@ -34,21 +34,27 @@ enum StatusBits : unsigned {
     ST_F16_RANGE = 2u,     // an FP16 snapshot value saturated
 };
 
-// The 24 distinct stencil coefficients of one destination point.  Each is
+// The distinct stencil coefficients of one destination point.  Each is
 // alpha*r + beta*r^2 with r = v^2 dt^2 at the destination (the reference's
-// v(j,i).^2*dt^2 and v(j,i).^4*dt^4 terms); for the three centre entries the
-// constant 2 is kept out and added exactly in the update.  The sign pattern
-// of the odd couplings is applied in mnad_update().
+// v(j,i).^2*dt^2 and v(j,i).^4*dt^4 terms).  The self-coupling blocks (Auu,
+// Avv, Aww) are applied in difference form, sum_k c_k (F_k - F_0), which is
+// exact for constant fields whatever the rounding of c_k; their centre
+// entries therefore reduce to
+//   Auu: 2 - sum_k c_k                        (the row sums to exactly 2)
+//   Avv: 2 - sum_k c_k + (-15 r/dx^2 + 15 r^2/dx^4)   -> K_VV_R
+//   Aww: 2 - sum_k c_k + (-15 r/dz^2 + 15 r^2/dz^4)   -> K_WW_R
+// (sums of Auu_gen.m:30-86, Avv_gen.m:101-157, Aww_gen.m:164-220).  The
+// sign pattern of the odd couplings is applied in mnad_update().
 enum Coef {
-    K_UU_Z, K_UU_X, K_UU_C, K_UU_D,          // Auu_gen.m
+    K_UU_Z, K_UU_X, K_UU_D,                  // Auu_gen.m
     K_UV_X1, K_UV_D, K_UV_X2,                // Auv_gen.m
     K_UW_Z1, K_UW_D, K_UW_Z2,                // Auw_gen.m
     K_VU_X1, K_VU_D,                         // Avu_gen.m
-    K_VV_Z, K_VV_X, K_VV_C, K_VV_D,          // Avv_gen.m
+    K_VV_Z, K_VV_X, K_VV_D, K_VV_R,          // Avv_gen.m
     K_VW,                                    // Avw_gen.m
     K_WU_Z1, K_WU_D,                         // Awu_gen.m
     K_WV,                                    // Awv_gen.m
-    K_WW_Z, K_WW_X, K_WW_C, K_WW_D,          // Aww_gen.m
+    K_WW_Z, K_WW_X, K_WW_D, K_WW_R,          // Aww_gen.m
     NCOEF
 };
 
@@ -109,19 +115,20 @@ struct Hood {
     float w00, wzm, wzp, wxm, wxp, wmm, wpm, wmp, wpp, wzm2, wzp2;
 };
 
-// Sigma_G A_FG * G without the exact "2*F" centre part, for F = U, V, W
-// (fwd_PDE_exact_MNAD.m:114-116).  Coefficient signs: the odd couplings use
-// one coefficient with the sign taken from the J index arrays of the
-// generator files (e.g. Auv_gen.m:119-170: +c at i+1, -c at i-1, +c at i-2).
+// su = nU - 2U + pU (likewise sv, sw) before the CPML term: the nine
+// products of fwd_PDE_exact_MNAD.m:114-116 minus the exact 2*F part, with the
+// self blocks in difference form.  Coefficient signs of the odd couplings
+// follow the J index arrays of the generator files (e.g. Auv_gen.m:119-170:
+// +c at i+1, -c at i-1, +c at i-2, -c at i+2).
 __device__ __forceinline__ void mnad_update(const PropDesc& P, float r, const Hood& h,
                                             float& su, float& sv, float& sw)
 {
     const float q = r * r;
     // nU row
-    float a = coef(P, K_UU_C, r, q) * h.u00;
-    a = fmaf(coef(P, K_UU_Z, r, q), h.uzm + h.uzp, a);
-    a = fmaf(coef(P, K_UU_X, r, q), h.uxm + h.uxp, a);
-    a = fmaf(P.beta[K_UU_D] * q, (h.umm + h.upp) + (h.upm + h.ump), a);
+    const float u2 = 2.0f * h.u00;
+    float a = coef(P, K_UU_Z, r, q) * ((h.uzm + h.uzp) - u2);
+    a = fmaf(coef(P, K_UU_X, r, q), (h.uxm + h.uxp) - u2, a);
+    a = fmaf(P.beta[K_UU_D] * q, ((h.umm + h.upp) + (h.upm + h.ump)) - 2.0f * u2, a);
     a = fmaf(coef(P, K_UV_X1, r, q), h.vxp - h.vxm, a);
     a = fmaf(P.beta[K_UV_D] * q, (h.vmp + h.vpp) - (h.vmm + h.vpm), a);
     a = fmaf(coef(P, K_UV_X2, r, q), h.vxm2 - h.vxp2, a);
@@ -130,19 +137,21 @@ __device__ __forceinline__ void mnad_update(const PropDesc& P, float r, const Ho
     a = fmaf(coef(P, K_UW_Z2, r, q), h.wzm2 - h.wzp2, a);
     su = a;
     // nV row
-    float b = coef(P, K_VV_C, r, q) * h.v00;
-    b = fmaf(coef(P, K_VV_Z, r, q), h.vzm + h.vzp, b);
-    b = fmaf(coef(P, K_VV_X, r, q), h.vxm + h.vxp, b);
-    b = fmaf(P.beta[K_VV_D] * q, (h.vmm + h.vpp) + (h.vpm + h.vmp), b);
+    const float v2 = 2.0f * h.v00;
+    float b = coef(P, K_VV_R, r, q) * h.v00;
+    b = fmaf(coef(P, K_VV_Z, r, q), (h.vzm + h.vzp) - v2, b);
+    b = fmaf(coef(P, K_VV_X, r, q), (h.vxm + h.vxp) - v2, b);
+    b = fmaf(P.beta[K_VV_D] * q, ((h.vmm + h.vpp) + (h.vpm + h.vmp)) - 2.0f * v2, b);
     b = fmaf(coef(P, K_VU_X1, r, q), h.uxm - h.uxp, b);
     b = fmaf(coef(P, K_VU_D, r, q), (h.umm + h.upm) - (h.ump + h.upp), b);
     b = fmaf(coef(P, K_VW, r, q), (h.wmm + h.wpp) - (h.wpm + h.wmp), b);
     sv = b;
     // nW row
-    float c = coef(P, K_WW_C, r, q) * h.w00;
-    c = fmaf(coef(P, K_WW_Z, r, q), h.wzm + h.wzp, c);
-    c = fmaf(coef(P, K_WW_X, r, q), h.wxm + h.wxp, c);
-    c = fmaf(P.beta[K_WW_D] * q, (h.wmm + h.wpp) + (h.wpm + h.wmp), c);
+    const float w2 = 2.0f * h.w00;
+    float c = coef(P, K_WW_R, r, q) * h.w00;
+    c = fmaf(coef(P, K_WW_Z, r, q), (h.wzm + h.wzp) - w2, c);
+    c = fmaf(coef(P, K_WW_X, r, q), (h.wxm + h.wxp) - w2, c);
+    c = fmaf(P.beta[K_WW_D] * q, ((h.wmm + h.wpp) + (h.wpm + h.wmp)) - 2.0f * w2, c);
     c = fmaf(coef(P, K_WU_Z1, r, q), h.uzm - h.uzp, c);
     c = fmaf(coef(P, K_WU_D, r, q), (h.umm + h.ump) - (h.upm + h.upp), c);
     c = fmaf(coef(P, K_WV, r, q), (h.vmm + h.vpp) - (h.vpm + h.vmp), c);

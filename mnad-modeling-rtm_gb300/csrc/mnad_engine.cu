@@ -138,7 +138,7 @@ int snapshot_T(int nt, int nf)
 }
 
 // Stencil coefficient polynomials alpha*r + beta*r^2 (r = v^2 dt^2) of the
-// nine generator files, centre entries without their constant 2.
+// nine generator files (see the Coef enum for the centre entries).
 static void stencil_polys(double dx, double dz, float* al, float* be)
 {
     const double dx2 = dx * dx, dz2 = dz * dz, dx3 = dx2 * dx, dz3 = dz2 * dz;
@@ -147,8 +147,6 @@ static void stencil_polys(double dx, double dz, float* al, float* be)
     // Auu_gen.m:30,37,44,65
     a[K_UU_Z] = (24.0 / 11) / dz2;   b[K_UU_Z] = -(15 / (11 * dz4) + 1 / (dx2 * dz2));
     a[K_UU_X] = (24.0 / 11) / dx2;   b[K_UU_X] = -(15 / (11 * dx4) + 1 / (dx2 * dz2));
-    a[K_UU_C] = -(48.0 / 11) * (1 / dx2 + 1 / dz2);
-    b[K_UU_C] = (30.0 / 11) * (1 / dx4 + 1 / dz4 + 11 / (15 * dx2 * dz2));
     b[K_UU_D] = 1 / (2 * dx2 * dz2);
     // Auv_gen.m:128 (i+1), 149 (diagonals at i+1), 163 (i-2)
     a[K_UV_X1] = (20.0 / 33) / dx;   b[K_UV_X1] = -(47 / (66 * dx3) + 1 / (6 * dx * dz2));
@@ -165,7 +163,9 @@ static void stencil_polys(double dx, double dz, float* al, float* be)
     // Avv_gen.m:101,108,115,136
     a[K_VV_Z] = 1 / dz2;             b[K_VV_Z] = -2 / (dx2 * dz2);
     a[K_VV_X] = -1.5 / dx2;          b[K_VV_X] = 5 / (2 * dx4) + 1 / (2 * dx2 * dz2);
-    a[K_VV_C] = -(12 / dx2 + 2 / dz2); b[K_VV_C] = 10 / dx4 + 4 / (dx2 * dz2);
+    // centre -(12/dx^2 + 2/dz^2) r + (10/dx^4 + 4/(dx^2 dz^2)) r^2 minus the
+    // off-diagonal sum: the residual of the difference form
+    a[K_VV_R] = -15 / dx2;           b[K_VV_R] = 15 / dx4;
     b[K_VV_D] = -1 / (4 * dx2 * dz2);
     // Avw_gen.m:192 ((j-1,i-1) and (j+1,i+1))
     a[K_VW] = -1 / (4 * dz * dx);    b[K_VW] = 1 / (4 * dz3 * dx);
@@ -178,7 +178,7 @@ static void stencil_polys(double dx, double dz, float* al, float* be)
     // Aww_gen.m:164,171,178,199
     a[K_WW_Z] = -1.5 / dz2;          b[K_WW_Z] = 5 / (2 * dz4) + 1 / (2 * dx2 * dz2);
     a[K_WW_X] = 1 / dx2;             b[K_WW_X] = -2 / (dz2 * dx2);
-    a[K_WW_C] = -(12 / dz2 + 2 / dx2); b[K_WW_C] = 10 / dz4 + 4 / (dx2 * dz2);
+    a[K_WW_R] = -15 / dz2;           b[K_WW_R] = 15 / dz4;
     b[K_WW_D] = -1 / (4 * dx2 * dz2);
     for (int k = 0; k < NCOEF; ++k) { al[k] = (float)a[k]; be[k] = (float)b[k]; }
 }

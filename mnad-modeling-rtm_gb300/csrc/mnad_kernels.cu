@@ -117,18 +117,19 @@ __device__ __forceinline__ void finish_point(const PropDesc& P, int tt, int tl, 
         sv = fmaf(-r, cv, sv);
         sw = fmaf(-r, cw, sw);
     }
-    float xu = fmaf(2.0f, h.u00, -pu) + su;
-    const float xv = fmaf(2.0f, h.v00, -pv) + sv;
-    const float xw = fmaf(2.0f, h.w00, -pw) + sw;
+    // nF = F + ((F - pF) + sF): one rounding at the field's magnitude.
+    float xu = h.u00 + ((h.u00 - pu) + su);
+    const float xv = h.v00 + ((h.v00 - pv) + sv);
+    const float xw = h.w00 + ((h.w00 - pw) + sw);
     const bool interior = (i >= d) & (i < P.nx - d) & (j >= d) & (j < P.nz - d);
     const int niz = P.nz - 2 * d;
     if (P.mode == MODE_FWD) {
         if (P.T > 0 && tt % P.T == 0 && interior) {
-            // fwd_PDE_exact_MNAD.m:128-141
-            float d2u;
-            if (tt == 1) d2u = xu;
-            else if (tt == 2) d2u = fmaf(-2.0f, h.u00, xu);
-            else d2u = fmaf(-2.0f, h.u00, xu) + pu;
+            // fwd_PDE_exact_MNAD.m:128-141 with nU - 2U + pU = su exactly:
+            // tt == 1 keeps nU (= 2U - pU + su), tt == 2 keeps nU - 2U.
+            float d2u = su;
+            if (tt == 1) d2u = fmaf(2.0f, h.u00, su - pu);
+            else if (tt == 2) d2u = su - pu;
             d2u *= P.inv_dt2;
             const size_t q = (size_t)(j - d) + (size_t)(i - d) * niz;
             const size_t nint = (size_t)niz * (P.nx - 2 * d);
