@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--plain-shots", type=int, default=2)
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, plain and CPU legs")
     ap.add_argument("--ref-steps", type=int, default=12, help="reference arm: time steps per worker sample")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "direct", "tma"])
     return ap.parse_args()
 
 
@@ -209,7 +210,7 @@ def run_ours(args):
     from mnad import workflow
     sv = workflow.config3(seed=rank, nshots=args.shots, nt=args.nt)
     jobs = workflow.shot_jobs(sv, "rtm")
-    ctx = mnad.Context(local, snapshot_codec=sv.codec)
+    ctx = mnad.Context(local, snapshot_codec=sv.codec, kernel=args.kernel)
     plan = ctx.plan(jobs)
     for _ in range(max(args.warmup, 0)):
         plan.run()
@@ -242,7 +243,8 @@ def run_ours(args):
         traffic = tr["bytes_per_point_update"] * pts / (plan.timing()["step_launches"])
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
-            "peak_kind": f"{peak_kind} hbm_gbs", "kernel": "mnad::step_direct",
+            "peak_kind": f"{peak_kind} hbm_gbs",
+            "kernel": "mnad::step_direct" if args.kernel == "direct" else "mnad::step_tma",
             "algorithmic_bytes_per_launch": abytes / plan.timing()["step_launches"]}
     plan.close()
     extras = {}

@@ -32,6 +32,7 @@ enum Pairing { PAIR_REFERENCE = 0, PAIR_ALIGNED = 1 };
 enum StatusBits : unsigned {
     ST_NONFINITE = 1u,     // a non-finite value was produced
     ST_F16_RANGE = 2u,     // an FP16 snapshot value saturated
+    ST_TIMEOUT = 4u,       // a bounded wait for a tile copy ran out
 };
 
 // The distinct stencil coefficients of one destination point.  Each is
@@ -73,7 +74,6 @@ struct PropDesc {
     float* mz;         // z-strip memory variables [side 2][var 9][nx][dpz]
     float kx, kz;      // 3 ln(1/R) / (2 D^3), D = d*dx or d*dz (C_cof.m:6,38)
     float dx, dz, dt, inv_dt;
-    float alpha[NCOEF], beta[NCOEF];
     // source (forward): storage offset of the point and the amount
     // r_src*w(tt) injected at each step (fwd_PDE_exact_MNAD.m:111)
     int src;                 // -1: none
@@ -102,10 +102,22 @@ struct PropDesc {
     unsigned* status;
 };
 
-__device__ __forceinline__ float coef(const PropDesc& P, int k, float r, float q)
-{
-    return fmaf(P.beta[k], q, P.alpha[k] * r);
-}
+// Stencil coefficient polynomials of one grid spacing (dx, dz): passed as
+// kernel parameters so the FMAs read them straight from the constant bank.
+struct Coefs {
+    float alpha[NCOEF], beta[NCOEF];
+};
+
+// Arguments of one step launch: the propagations of one (dx, dz) group.
+struct StepArgs {
+    Coefs coef;
+    const PropDesc* props;
+    const int* tile_prop;
+    const void* tmaps;     // CUtensorMap[nprops][TMAPS_PER_PROP] (TMA kernel)
+    const int4* tile_info; // per tile: propagation, j0, i0, flags (TMA kernel)
+    int ntiles;
+    int s;                 // global step index
+};
 
 // Neighbourhood of one point for the three fields.  Naming: <f><z><x> with
 // z/x in {m: -1, 0: 0, p: +1}; the x+-2 (V) and z+-2 (W) reaches are extra.
@@ -116,46 +128,94 @@ struct Hood {
 };
 
 // su = nU - 2U + pU (likewise sv, sw) before the CPML term: the nine
-// products of fwd_PDE_exact_MNAD.m:114-116 minus the exact 2*F part, with the
-// self blocks in difference form.  Coefficient signs of the odd couplings
-// follow the J index arrays of the generator files (e.g. Auv_gen.m:119-170:
-// +c at i+1, -c at i-1, +c at i-2, -c at i+2).
-__device__ __forceinline__ void mnad_update(const PropDesc& P, float r, const Hood& h,
+// products of fwd_PDE_exact_MNAD.m:114-116 minus the exact 2*F part.  The
+// self blocks are taken in difference form, every coefficient is
+// alpha_k r + beta_k r^2, and each row is evaluated as
+//     r * sum_k alpha_k D_k + r^2 * sum_k beta_k D_k
+// over the neighbour combinations D_k (two FMAs per term, constants from the
+// kernel parameters).  Signs of the odd couplings follow the J index arrays
+// of the generator files (e.g. Auv_gen.m:119-170: +c at i+1, -c at i-1,
+// +c at i-2, -c at i+2).
+__device__ __forceinline__ void mnad_update(const Coefs& K, float r, const Hood& h,
                                             float& su, float& sv, float& sw)
 {
     const float q = r * r;
+    const float* a = K.alpha;
+    const float* b = K.beta;
+    // U combinations
+    const float u2 = h.u00 + h.u00;
+    const float dUz = (h.uzm + h.uzp) - u2, dUx = (h.uxm + h.uxp) - u2;
+    const float uA = h.umm + h.upp, uB = h.upm + h.ump;
+    const float dUd = (uA + uB) - (u2 + u2);
+    const float uLx = h.uxm - h.uxp;                          // Avu_gen.m:30,37
+    const float uLz = h.uzm - h.uzp;                          // Awu_gen.m:29,36
+    const float uDx = (h.umm + h.upm) - (h.ump + h.upp);      // Avu_gen.m:44-65
+    const float uDz = (h.umm + h.ump) - (h.upm + h.upp);      // Awu_gen.m:44-67
+    // V combinations
+    const float v2 = h.v00 + h.v00;
+    const float dVz = (h.vzm + h.vzp) - v2, dVx = (h.vxm + h.vxp) - v2;
+    const float vA = h.vmm + h.vpp, vB = h.vpm + h.vmp;
+    const float dVd = (vA + vB) - (v2 + v2);
+    const float vX1 = h.vxp - h.vxm;                          // Auv_gen.m:121,128
+    const float vDx = (h.vmp + h.vpp) - (h.vmm + h.vpm);      // Auv_gen.m:135-156
+    const float vX2 = h.vxm2 - h.vxp2;                        // Auv_gen.m:163,170
+    const float vXZ = vA - vB;                                // Awv_gen.m:106-127
+    // W combinations
+    const float w2 = h.w00 + h.w00;
+    const float dWz = (h.wzm + h.wzp) - w2, dWx = (h.wxm + h.wxp) - w2;
+    const float wA = h.wmm + h.wpp, wB = h.wpm + h.wmp;
+    const float dWd = (wA + wB) - (w2 + w2);
+    const float wZ1 = h.wzp - h.wzm;                          // Auw_gen.m:205,212
+    const float wDz = (h.wpm + h.wpp) - (h.wmm + h.wmp);      // Auw_gen.m:219-240
+    const float wZ2 = h.wzm2 - h.wzp2;                        // Auw_gen.m:247,254
+    const float wXZ = wA - wB;                                // Avw_gen.m:192-213
     // nU row
-    const float u2 = 2.0f * h.u00;
-    float a = coef(P, K_UU_Z, r, q) * ((h.uzm + h.uzp) - u2);
-    a = fmaf(coef(P, K_UU_X, r, q), (h.uxm + h.uxp) - u2, a);
-    a = fmaf(P.beta[K_UU_D] * q, ((h.umm + h.upp) + (h.upm + h.ump)) - 2.0f * u2, a);
-    a = fmaf(coef(P, K_UV_X1, r, q), h.vxp - h.vxm, a);
-    a = fmaf(P.beta[K_UV_D] * q, (h.vmp + h.vpp) - (h.vmm + h.vpm), a);
-    a = fmaf(coef(P, K_UV_X2, r, q), h.vxm2 - h.vxp2, a);
-    a = fmaf(coef(P, K_UW_Z1, r, q), h.wzp - h.wzm, a);
-    a = fmaf(P.beta[K_UW_D] * q, (h.wpm + h.wpp) - (h.wmm + h.wmp), a);
-    a = fmaf(coef(P, K_UW_Z2, r, q), h.wzm2 - h.wzp2, a);
-    su = a;
+    float ra = a[K_UU_Z] * dUz;
+    ra = fmaf(a[K_UU_X], dUx, ra);
+    ra = fmaf(a[K_UV_X1], vX1, ra);
+    ra = fmaf(a[K_UV_X2], vX2, ra);
+    ra = fmaf(a[K_UW_Z1], wZ1, ra);
+    ra = fmaf(a[K_UW_Z2], wZ2, ra);
+    float qa = b[K_UU_Z] * dUz;
+    qa = fmaf(b[K_UU_X], dUx, qa);
+    qa = fmaf(b[K_UU_D], dUd, qa);
+    qa = fmaf(b[K_UV_X1], vX1, qa);
+    qa = fmaf(b[K_UV_D], vDx, qa);
+    qa = fmaf(b[K_UV_X2], vX2, qa);
+    qa = fmaf(b[K_UW_Z1], wZ1, qa);
+    qa = fmaf(b[K_UW_D], wDz, qa);
+    qa = fmaf(b[K_UW_Z2], wZ2, qa);
+    su = fmaf(q, qa, r * ra);
     // nV row
-    const float v2 = 2.0f * h.v00;
-    float b = coef(P, K_VV_R, r, q) * h.v00;
-    b = fmaf(coef(P, K_VV_Z, r, q), (h.vzm + h.vzp) - v2, b);
-    b = fmaf(coef(P, K_VV_X, r, q), (h.vxm + h.vxp) - v2, b);
-    b = fmaf(P.beta[K_VV_D] * q, ((h.vmm + h.vpp) + (h.vpm + h.vmp)) - 2.0f * v2, b);
-    b = fmaf(coef(P, K_VU_X1, r, q), h.uxm - h.uxp, b);
-    b = fmaf(coef(P, K_VU_D, r, q), (h.umm + h.upm) - (h.ump + h.upp), b);
-    b = fmaf(coef(P, K_VW, r, q), (h.wmm + h.wpp) - (h.wpm + h.wmp), b);
-    sv = b;
+    float rb = a[K_VV_Z] * dVz;
+    rb = fmaf(a[K_VV_X], dVx, rb);
+    rb = fmaf(a[K_VV_R], h.v00, rb);
+    rb = fmaf(a[K_VU_X1], uLx, rb);
+    rb = fmaf(a[K_VU_D], uDx, rb);
+    rb = fmaf(a[K_VW], wXZ, rb);
+    float qb = b[K_VV_Z] * dVz;
+    qb = fmaf(b[K_VV_X], dVx, qb);
+    qb = fmaf(b[K_VV_D], dVd, qb);
+    qb = fmaf(b[K_VV_R], h.v00, qb);
+    qb = fmaf(b[K_VU_X1], uLx, qb);
+    qb = fmaf(b[K_VU_D], uDx, qb);
+    qb = fmaf(b[K_VW], wXZ, qb);
+    sv = fmaf(q, qb, r * rb);
     // nW row
-    const float w2 = 2.0f * h.w00;
-    float c = coef(P, K_WW_R, r, q) * h.w00;
-    c = fmaf(coef(P, K_WW_Z, r, q), (h.wzm + h.wzp) - w2, c);
-    c = fmaf(coef(P, K_WW_X, r, q), (h.wxm + h.wxp) - w2, c);
-    c = fmaf(P.beta[K_WW_D] * q, ((h.wmm + h.wpp) + (h.wpm + h.wmp)) - 2.0f * w2, c);
-    c = fmaf(coef(P, K_WU_Z1, r, q), h.uzm - h.uzp, c);
-    c = fmaf(coef(P, K_WU_D, r, q), (h.umm + h.ump) - (h.upm + h.upp), c);
-    c = fmaf(coef(P, K_WV, r, q), (h.vmm + h.vpp) - (h.vpm + h.vmp), c);
-    sw = c;
+    float rc = a[K_WW_Z] * dWz;
+    rc = fmaf(a[K_WW_X], dWx, rc);
+    rc = fmaf(a[K_WW_R], h.w00, rc);
+    rc = fmaf(a[K_WU_Z1], uLz, rc);
+    rc = fmaf(a[K_WU_D], uDz, rc);
+    rc = fmaf(a[K_WV], vXZ, rc);
+    float qc = b[K_WW_Z] * dWz;
+    qc = fmaf(b[K_WW_X], dWx, qc);
+    qc = fmaf(b[K_WW_D], dWd, qc);
+    qc = fmaf(b[K_WW_R], h.w00, qc);
+    qc = fmaf(b[K_WU_Z1], uLz, qc);
+    qc = fmaf(b[K_WU_D], uDz, qc);
+    qc = fmaf(b[K_WV], vXZ, qc);
+    sw = fmaf(q, qc, r * rc);
 }
 
 // CPML coefficients of C_cof.m:6-16 at one strip point.  X is the distance

@@ -2,6 +2,9 @@
 #include "mnad_engine.h"
 #include "mnad_kernels.h"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -49,6 +52,7 @@ Context::Context(int dev, size_t budget_bytes) : device(dev), budget(budget_byte
     MNAD_CK(cudaDeviceGetDefaultMemPool(&pool, dev));
     uint64_t keep = UINT64_MAX;   // keep freed blocks cached for the next job
     MNAD_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    MNAD_CK(cudaFuncSetAttribute(step_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_tma_smem_bytes()));
     MNAD_CK(cudaMalloc(&d_status, sizeof(unsigned)));
     MNAD_CK(cudaMemset(d_status, 0, sizeof(unsigned)));
     opt.snapshot_codec = MNAD_SNAP_F32;
@@ -110,8 +114,39 @@ void download(Context& ctx, void* dst, const void* src, size_t bytes)
 // ---------------------------------------------------------------------------
 TileCfg tile_cfg(int kernel)
 {
-    (void)kernel;
-    return TileCfg{MNAD_KERNEL_DIRECT, DIRECT_TZ, DIRECT_TX};
+    if (kernel == MNAD_KERNEL_DIRECT) return TileCfg{MNAD_KERNEL_DIRECT, DIRECT_TZ, DIRECT_TX};
+    return TileCfg{MNAD_KERNEL_TMA, TMA_TZ, TMA_TX};
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda, so the library loads on hosts without a driver).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q{};
+        void* p = nullptr;
+        MNAD_CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !p) throw Error(MNAD_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 2-D map over one field's padded storage (inner dimension z, ld rows, nx+2HX
+// columns) with a box of bz rows x bx columns.
+static CUtensorMap field_map(const float* base, int ld, int ncols, int bz, int bx)
+{
+    CUtensorMap m;
+    cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)ncols};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+    cuuint32_t box[2] = {(cuuint32_t)bz, (cuuint32_t)bx};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
+                                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(MNAD_E_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return m;
 }
 
 void model_minmax(const double* v, size_t n, double& vmin, double& vmax)
@@ -231,7 +266,7 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     }
     D.dx = (float)s.dx; D.dz = (float)s.dz; D.dt = (float)s.dt; D.inv_dt = (float)(1.0 / s.dt);
     D.inv_dt2 = (float)(1.0 / (s.dt * s.dt));
-    stencil_polys(s.dx, s.dz, D.alpha, D.beta);
+    stencil_polys(s.dx, s.dz, coefs.alpha, coefs.beta);
     D.status = ctx.d_status;
 
     auto off = [&](int j, int i) { return (int)((size_t)(i + HX) * ld + (j + HZ)); };
@@ -262,6 +297,7 @@ void Prop::build(Context& ctx, const TileCfg& tc)
         rr[e] = r_of(s.v[(size_t)s.zr[k] + (size_t)s.xr[k] * nz], s.dt, s.mode);
     }
     D.nr = nr;
+    tile_rec_host = cnt;
     tile_rec = DevMem(&ctx, (ntiles + 1) * sizeof(int));
     upload(ctx, tile_rec.get(), cnt.data(), (ntiles + 1) * sizeof(int));
     D.tile_rec = tile_rec.as<int>();
@@ -338,34 +374,96 @@ Batch::~Batch()
 
 void Batch::finalize()
 {
-    std::vector<PropDesc> descs;
-    std::vector<int> tile_prop;
+    groups_.clear();
     nsteps_ = 0;
-    for (size_t k = 0; k < props_.size(); ++k) {
-        PropDesc& D = props_[k]->desc;
-        D.tile_base = (int)tile_prop.size();
-        tile_prop.insert(tile_prop.end(), (size_t)D.ntz * D.ntx, (int)k);
-        descs.push_back(D);
-        nsteps_ = std::max(nsteps_, D.nt);
+    ntiles_ = 0;
+    std::vector<PropDesc> all;
+    for (Prop* p : props_) {
+        LaunchGroup* g = nullptr;
+        for (auto& x : groups_)
+            if (x->dx == p->spec.dx && x->dz == p->spec.dz) g = x.get();
+        if (!g) {
+            groups_.push_back(std::make_unique<LaunchGroup>());
+            g = groups_.back().get();
+            g->dx = p->spec.dx;
+            g->dz = p->spec.dz;
+            g->coefs = p->coefs;
+        }
+        g->props.push_back(p);
+        nsteps_ = std::max(nsteps_, p->spec.nt);
     }
-    ntiles_ = (int)tile_prop.size();
-    d_desc_ = DevMem(&ctx_, std::max<size_t>(1, descs.size()) * sizeof(PropDesc));
-    d_tile_prop_ = DevMem(&ctx_, std::max<size_t>(1, tile_prop.size()) * sizeof(int));
-    upload(ctx_, d_desc_.get(), descs.data(), descs.size() * sizeof(PropDesc));
-    upload(ctx_, d_tile_prop_.get(), tile_prop.data(), tile_prop.size() * sizeof(int));
+    for (auto& g : groups_) {
+        std::vector<PropDesc> descs;
+        std::vector<int> tile_prop;
+        std::vector<int4> info;
+        std::vector<CUtensorMap> maps;
+        for (size_t k = 0; k < g->props.size(); ++k) {
+            Prop* p = g->props[k];
+            PropDesc& D = p->desc;
+            D.tile_base = (int)tile_prop.size();
+            tile_prop.insert(tile_prop.end(), (size_t)D.ntz * D.ntx, (int)k);
+            descs.push_back(D);
+            all.push_back(D);
+            if (tc_.kind != MNAD_KERNEL_TMA) continue;
+            const int ncols = D.nx + 2 * HX;
+            for (int t = 0; t < 2; ++t)
+                for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ + 8, TMA_TX + 4));
+            for (int t = 0; t < 2; ++t)
+                for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ, TMA_TX));
+            maps.push_back(field_map(D.r, D.ld, ncols, TMA_TZ, TMA_TX));
+            for (int tx = 0; tx < D.ntx; ++tx)
+                for (int tz = 0; tz < D.ntz; ++tz) {
+                    const int j0 = tz * TMA_TZ, i0 = tx * TMA_TX, d = D.d;
+                    const bool interior = j0 >= d && j0 + TMA_TZ <= D.nz - d && i0 >= d && i0 + TMA_TX <= D.nx - d;
+                    const int tl = tz + tx * D.ntz;
+                    const bool rec = p->tile_rec_host[tl + 1] > p->tile_rec_host[tl];
+                    info.push_back(make_int4((int)k, j0, i0, (interior ? 0 : TILE_STRIP) | (rec ? TILE_RECEIVERS : 0)));
+                }
+        }
+        g->ntiles = (int)tile_prop.size();
+        ntiles_ += g->ntiles;
+        g->desc = DevMem(&ctx_, descs.size() * sizeof(PropDesc));
+        g->tile_prop = DevMem(&ctx_, std::max<size_t>(1, tile_prop.size()) * sizeof(int));
+        upload(ctx_, g->desc.get(), descs.data(), descs.size() * sizeof(PropDesc));
+        upload(ctx_, g->tile_prop.get(), tile_prop.data(), tile_prop.size() * sizeof(int));
+        if (!maps.empty()) {
+            g->tmaps = DevMem(&ctx_, maps.size() * sizeof(CUtensorMap));
+            upload(ctx_, g->tmaps.get(), maps.data(), maps.size() * sizeof(CUtensorMap));
+            g->tile_info = DevMem(&ctx_, info.size() * sizeof(int4));
+            upload(ctx_, g->tile_info.get(), info.data(), info.size() * sizeof(int4));
+        }
+    }
+    d_all_desc_ = DevMem(&ctx_, std::max<size_t>(1, all.size()) * sizeof(PropDesc));
+    upload(ctx_, d_all_desc_.get(), all.data(), all.size() * sizeof(PropDesc));
 }
 
 void Batch::launch_step(int s)
 {
-    dim3 block(DIRECT_TZ, DIRECT_TX);
-    step_direct<<<ntiles_, block, 0, ctx_.stream>>>(d_desc_.as<PropDesc>(), d_tile_prop_.as<int>(), s);
+    for (auto& g : groups_) {
+        if (g->ntiles == 0) continue;
+        StepArgs a;
+        a.coef = g->coefs;
+        a.props = g->desc.as<PropDesc>();
+        a.tile_prop = g->tile_prop.as<int>();
+        a.tmaps = g->tmaps.get();
+        a.tile_info = g->tile_info.as<int4>();
+        a.ntiles = g->ntiles;
+        a.s = s;
+        if (tc_.kind == MNAD_KERNEL_TMA) {
+            const size_t smem = step_tma_smem_bytes();
+            const int grid = std::min(g->ntiles, ctx_.num_sms * TMA_CTAS_PER_SM);
+            step_tma<<<grid, TMA_TZY * TMA_TX, smem, ctx_.stream>>>(a);
+        } else
+            step_direct<<<g->ntiles, dim3(DIRECT_TZ, DIRECT_TX), 0, ctx_.stream>>>(a);
+    }
 }
 
 void Batch::start()
 {
     for (Prop* p : props_) p->reset(ctx_);
     if (!props_.empty())
-        seed_sources<<<((int)props_.size() + 127) / 128, 128, 0, ctx_.stream>>>(d_desc_.as<PropDesc>(), (int)props_.size());
+        seed_sources<<<((int)props_.size() + 127) / 128, 128, 0, ctx_.stream>>>(d_all_desc_.as<PropDesc>(),
+                                                                            (int)props_.size());
     MNAD_CK(cudaGetLastError());
 }
 

@@ -98,7 +98,9 @@ struct PropSpec {
 struct Prop {
     PropSpec spec;
     PropDesc desc{};
+    Coefs coefs{};                     // stencil polynomials of (dx, dz)
     size_t S = 0;                      // floats per field in storage
+    std::vector<int> tile_rec_host;    // receiver bucket offsets per tile
     DevMem fields, r, mx, mz, src_amp, rec_pt, rec_id, rec_r, tile_rec, data, datav, dataw, image;
     void build(Context& ctx, const TileCfg& tc);
     void reset(Context& ctx);          // zero the state of a fresh run (stream-ordered)
@@ -107,7 +109,17 @@ struct Prop {
     double algorithmic_bytes() const;
 };
 
-// Propagations that advance together: one launch per time step.
+// Propagations of one grid spacing (dx, dz) share the stencil coefficients
+// that a launch carries as kernel parameters.
+struct LaunchGroup {
+    Coefs coefs{};
+    double dx = 0, dz = 0;
+    std::vector<Prop*> props;
+    DevMem desc, tile_prop, tmaps, tile_info;
+    int ntiles = 0;
+};
+
+// Propagations that advance together: one launch per (dx, dz) group and step.
 class Batch {
 public:
     Batch(Context& ctx, const TileCfg& tc) : ctx_(ctx), tc_(tc) {}
@@ -125,7 +137,8 @@ private:
     Context& ctx_;
     TileCfg tc_;
     std::vector<Prop*> props_;
-    DevMem d_desc_, d_tile_prop_;
+    std::vector<std::unique_ptr<LaunchGroup>> groups_;
+    DevMem d_all_desc_;                // every descriptor (source seeding)
     int ntiles_ = 0, nsteps_ = 0;
     cudaGraphExec_t graph_ = nullptr;
 };

@@ -9,7 +9,24 @@ namespace mnad {
 constexpr int DIRECT_TZ = 32;
 constexpr int DIRECT_TX = 8;
 
-__global__ void step_direct(const PropDesc* __restrict__ props, const int* __restrict__ tile_prop, int s);
+// Tile of the TMA step kernel: TMA_TZY x TMA_TX threads, TMA_PZ consecutive
+// z points per thread.
+constexpr int TMA_TZY = 16;
+constexpr int TMA_TX = 16;
+constexpr int TMA_PZ = 4;
+constexpr int TMA_TZ = TMA_TZY * TMA_PZ;
+constexpr int TMA_STAGES = 3;         // tiles in flight per CTA
+constexpr int TMA_CTAS_PER_SM = 2;
+// Tensor maps of one propagation: halo boxes of U,V,W at both time levels,
+// point boxes of U,V,W at both levels, point box of r.
+constexpr int TMAP_HALO = 0, TMAP_POINT = 6, TMAP_R = 12, TMAPS_PER_PROP = 13;
+// tile_info.w flags
+constexpr int TILE_STRIP = 1;         // intersects a CPML strip or the grid edge
+constexpr int TILE_RECEIVERS = 2;     // has receivers
+
+__global__ void step_direct(const __grid_constant__ StepArgs A);
+__global__ void step_tma(const __grid_constant__ StepArgs A);
+size_t step_tma_smem_bytes();
 __global__ void build_r(const double* __restrict__ v, int nz, int nx, double dt, int adjoint,
                         float* __restrict__ r, int ld);
 __global__ void seed_sources(const PropDesc* __restrict__ props, int n);

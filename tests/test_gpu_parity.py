@@ -236,3 +236,20 @@ def test_errors_are_reported_not_crashed(ctx):
     # the context stays usable after every error
     out = ctx.fwd(10.0, 5, [1, 2], 10.0, 5, [1, 2], v, 1e-3, 10, np.ones(10), 4)
     assert np.all(np.isfinite(out))
+
+
+@pytest.mark.parametrize("kernel", ["direct", "tma"])
+def test_step_kernels_agree(ctx, kernel):
+    """Both step kernels evaluate the same per-point arithmetic."""
+    g = np.load(os.path.join(GOLDEN, "golden_rtm_small.npz"))
+    dx, dz, dt, nt, d = float(g["dx"]), float(g["dz"]), float(g["dt"]), int(g["nt"]), int(g["d"])
+    ctx.set_options(kernel=kernel)
+    try:
+        data = ctx.fwd(dx, int(g["xs"]), g["xr"], dz, int(g["zs"]), g["zr"], g["v"], dt, nt, g["w"], d, ss=8)
+        bg = ctx.fwd(dx, int(g["xs"]), g["xr"], dz, int(g["zs"]), g["zr"], g["vs"], dt, nt, g["w"], d, ss=8, indx=1)
+        im = ctx.adj(dx, dz, nt, dt, g["vs"], g["xr"], g["zr"], data - bg, d, ss=8)
+    finally:
+        ctx.set_options(kernel="auto")
+    assert rel(data, g["datau"]) <= TOL_GATHER
+    assert rel(im, g["Im"]) <= TOL_IMAGE
+    ctx.wavefield_release(8)
