@@ -229,6 +229,7 @@ def run_ours(args):
     barrier_sync(world)
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
+    status = ctx.status()
     pts, abytes = plan.work()
     total_s = allmax(sum(run_ms) / 1e3, world)
     pts_all = allsum(pts * args.steps, world)
@@ -279,7 +280,7 @@ def run_ours(args):
                            "snapshots": sv.codec, "image": "f64", "parallelism": f"replicas x{world}",
                            "l2": "state per step >> L2 (inputs larger than L2)"},
                 "shots_per_hr": round(shots_hr, 1), "roofline": roof, "clocks": clocks,
-                "gpu_launches": launches, "wall_s": round(wall, 2)}
+                "gpu_launches": launches, "wall_s": round(wall, 2), "device_status": status}
         line.update(extras)
         if "plain" in extras:
             line["batched_vs_plain"] = round(value / extras["plain"]["value"], 2)

@@ -59,19 +59,22 @@ enum Coef {
     NCOEF
 };
 
-struct PropDesc {
+// 16-byte aligned (and sized) so a CTA can fetch it with one bulk copy.
+struct __align__(16) PropDesc {
     int mode;          // MODE_FWD / MODE_ADJ
     int nt;            // steps of this propagation
     int nz, nx;        // padded grid (as passed to the reference)
     int ld;            // z pitch of per-point storage (floats)
     int d;             // CPML thickness (d_pml)
-    int dpz;           // pitch of one z-strip column (floats, >= d)
+    int dpz;           // pitch of one z-strip column (floats, >= d + 6, multiple of 4)
+    int zb0;           // first storage row of the bottom z strip: (nz - d) rounded down to 4
     int tile_base;     // first global tile of this propagation
     int ntz, ntx;      // tiles along z / x
     float* fld[2][3];  // [time level][U,V,W], storage origin (halo included)
     const float* r;    // v^2 dt^2, same storage
     float* mx;         // x-strip memory variables [side 2][var 9][d][ld]
-    float* mz;         // z-strip memory variables [side 2][var 9][nx][dpz]
+    float* mz;         // z-strip memory variables [side 2][var 9][nx][dpz]; top side slot k
+                       // holds row k, bottom side slot k holds row zb0 + k
     float kx, kz;      // 3 ln(1/R) / (2 D^3), D = d*dx or d*dz (C_cof.m:6,38)
     float dx, dz, dt, inv_dt;
     // source (forward): storage offset of the point and the amount
@@ -114,8 +117,11 @@ struct StepArgs {
     const PropDesc* props;
     const int* tile_prop;
     const void* tmaps;     // CUtensorMap[nprops][TMAPS_PER_PROP] (TMA kernel)
-    const int4* tile_info; // per tile: propagation, j0, i0, flags (TMA kernel)
+    const int4* tile_info; // per tile: receiver bucket begin/end, flags (TMA kernel)
+    int* tile_counter;     // tiles claimed so far in this launch (TMA kernel, zeroed per run)
     int ntiles;
+    int ntz;               // tiles along z of every propagation of the group
+    int tiles_per_prop;    // ntz * ntx (one geometry per launch group)
     int s;                 // global step index
 };
 

@@ -230,7 +230,10 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     const int nz = s.nz, nx = s.nx, d = s.d;
     const int ld = (int)round_up((size_t)nz + HZ + HZB, 32);
     S = (size_t)ld * (nx + 2 * HX);
-    const int dpz = (int)round_up((size_t)std::max(d, 1), 4);
+    // z-strip columns hold d rows plus room for the 4-row groups of the TMA
+    // kernel that overhang the strip (aligned to 16 bytes at both sides).
+    const int dpz = (int)round_up((size_t)d + 6, 4);
+    const int zb0 = (nz - d) & ~3;
     cudaStream_t st = ctx.stream;
 
     fields = DevMem(&ctx, 6 * S * sizeof(float));
@@ -251,7 +254,7 @@ void Prop::build(Context& ctx, const TileCfg& tc)
 
     PropDesc& D = desc;
     std::memset(&D, 0, sizeof(D));
-    D.mode = s.mode; D.nt = s.nt; D.nz = nz; D.nx = nx; D.ld = ld; D.d = d; D.dpz = dpz;
+    D.mode = s.mode; D.nt = s.nt; D.nz = nz; D.nx = nx; D.ld = ld; D.d = d; D.dpz = dpz; D.zb0 = zb0;
     D.ntz = (nz + tc.tz - 1) / tc.tz;
     D.ntx = (nx + tc.tx - 1) / tc.tx;
     for (int t = 0; t < 2; ++t)
@@ -381,12 +384,17 @@ void Batch::finalize()
     for (Prop* p : props_) {
         LaunchGroup* g = nullptr;
         for (auto& x : groups_)
-            if (x->dx == p->spec.dx && x->dz == p->spec.dz) g = x.get();
+            if (x->dx == p->spec.dx && x->dz == p->spec.dz && x->nz == p->spec.nz && x->nx == p->spec.nx &&
+                x->d == p->spec.d)
+                g = x.get();
         if (!g) {
             groups_.push_back(std::make_unique<LaunchGroup>());
             g = groups_.back().get();
             g->dx = p->spec.dx;
             g->dz = p->spec.dz;
+            g->nz = p->spec.nz;
+            g->nx = p->spec.nx;
+            g->d = p->spec.d;
             g->coefs = p->coefs;
         }
         g->props.push_back(p);
@@ -416,8 +424,8 @@ void Batch::finalize()
                     const int j0 = tz * TMA_TZ, i0 = tx * TMA_TX, d = D.d;
                     const bool interior = j0 >= d && j0 + TMA_TZ <= D.nz - d && i0 >= d && i0 + TMA_TX <= D.nx - d;
                     const int tl = tz + tx * D.ntz;
-                    const bool rec = p->tile_rec_host[tl + 1] > p->tile_rec_host[tl];
-                    info.push_back(make_int4((int)k, j0, i0, (interior ? 0 : TILE_STRIP) | (rec ? TILE_RECEIVERS : 0)));
+                    const int rb = p->tile_rec_host[tl], re = p->tile_rec_host[tl + 1];
+                    info.push_back(make_int4(rb, re, (interior ? 0 : TILE_STRIP) | (re > rb ? TILE_RECEIVERS : 0), tl));
                 }
         }
         g->ntiles = (int)tile_prop.size();
@@ -433,13 +441,16 @@ void Batch::finalize()
             upload(ctx_, g->tile_info.get(), info.data(), info.size() * sizeof(int4));
         }
     }
+    if (tc_.kind == MNAD_KERNEL_TMA)
+        d_counters_ = DevMem(&ctx_, std::max<size_t>(1, (size_t)nsteps_ * groups_.size()) * sizeof(int));
     d_all_desc_ = DevMem(&ctx_, std::max<size_t>(1, all.size()) * sizeof(PropDesc));
     upload(ctx_, d_all_desc_.get(), all.data(), all.size() * sizeof(PropDesc));
 }
 
 void Batch::launch_step(int s)
 {
-    for (auto& g : groups_) {
+    for (size_t gi = 0; gi < groups_.size(); ++gi) {
+        auto& g = groups_[gi];
         if (g->ntiles == 0) continue;
         StepArgs a;
         a.coef = g->coefs;
@@ -447,7 +458,10 @@ void Batch::launch_step(int s)
         a.tile_prop = g->tile_prop.as<int>();
         a.tmaps = g->tmaps.get();
         a.tile_info = g->tile_info.as<int4>();
+        a.tile_counter = d_counters_.as<int>() + (d_counters_.get() ? (size_t)s * groups_.size() + gi : 0);
         a.ntiles = g->ntiles;
+        a.ntz = g->props.empty() ? 0 : g->props[0]->desc.ntz;
+        a.tiles_per_prop = g->props.empty() ? 0 : g->props[0]->desc.ntz * g->props[0]->desc.ntx;
         a.s = s;
         if (tc_.kind == MNAD_KERNEL_TMA) {
             const size_t smem = step_tma_smem_bytes();
@@ -461,6 +475,7 @@ void Batch::launch_step(int s)
 void Batch::start()
 {
     for (Prop* p : props_) p->reset(ctx_);
+    if (d_counters_.get()) MNAD_CK(cudaMemsetAsync(d_counters_.get(), 0, d_counters_.size(), ctx_.stream));
     if (!props_.empty())
         seed_sources<<<((int)props_.size() + 127) / 128, 128, 0, ctx_.stream>>>(d_all_desc_.as<PropDesc>(),
                                                                             (int)props_.size());

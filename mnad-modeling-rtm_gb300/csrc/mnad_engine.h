@@ -109,17 +109,18 @@ struct Prop {
     double algorithmic_bytes() const;
 };
 
-// Propagations of one grid spacing (dx, dz) share the stencil coefficients
-// that a launch carries as kernel parameters.
+// Propagations of one geometry (dx, dz, nz, nx, d_pml) share the stencil
+// coefficients that a launch carries as kernel parameters and one tiling.
 struct LaunchGroup {
     Coefs coefs{};
     double dx = 0, dz = 0;
+    int nz = 0, nx = 0, d = 0;
     std::vector<Prop*> props;
     DevMem desc, tile_prop, tmaps, tile_info;
     int ntiles = 0;
 };
 
-// Propagations that advance together: one launch per (dx, dz) group and step.
+// Propagations that advance together: one launch per geometry group and step.
 class Batch {
 public:
     Batch(Context& ctx, const TileCfg& tc) : ctx_(ctx), tc_(tc) {}
@@ -139,6 +140,7 @@ private:
     std::vector<Prop*> props_;
     std::vector<std::unique_ptr<LaunchGroup>> groups_;
     DevMem d_all_desc_;                // every descriptor (source seeding)
+    DevMem d_counters_;                // per step and group: tiles claimed (TMA kernel)
     int ntiles_ = 0, nsteps_ = 0;
     cudaGraphExec_t graph_ = nullptr;
 };

@@ -59,7 +59,7 @@ __device__ __forceinline__ void cpml_point(const PropDesc& P, int j, int i, floa
     }
     if (j < d || j >= P.nz - d) {
         const int side = j < d ? 0 : 1;
-        const int k = side ? j - (P.nz - d) : j;
+        const int k = side ? j - P.zb0 : j;
         const float X = side ? float(k + 1) * P.dz : float(d - j) * P.dz;
         float c1, c2, c3;
         cpml_coefs(P.kz, vel, X, P.dt, c1, c2, c3);

@@ -253,3 +253,24 @@ def test_step_kernels_agree(ctx, kernel):
     assert rel(data, g["datau"]) <= TOL_GATHER
     assert rel(im, g["Im"]) <= TOL_IMAGE
     ctx.wavefield_release(8)
+
+
+@pytest.mark.parametrize("kernel", ["direct", "tma"])
+@pytest.mark.parametrize("nz,nx,d", [(48, 64, 0), (45, 53, 1), (66, 47, 5), (80, 80, 40)])
+def test_edge_geometries(ctx, kernel, nz, nx, d):
+    """No CPML, a 1-point CPML, sizes off the tile and 4-row grid, nz = 2*d_pml."""
+    rng = np.random.default_rng(nz * 1000 + nx + d)
+    v = 1800 + 600 * rng.random((nz, nx))
+    nt = 120
+    w = workflow.ricker(35.0, 1e-3, nt)
+    xr = np.arange(1, nx + 1, 2)
+    zr = np.full(xr.size, d + 1)      # first interior row, as the reference drivers place them
+    zs, xs = nz // 2, nx // 2
+    ctx.set_options(kernel=kernel)
+    try:
+        out = ctx.fwd(10.0, xs, xr, 10.0, zs, zr, v, 1e-3, nt, w, d)
+    finally:
+        ctx.set_options(kernel="auto")
+    ref = coracle.fwd(10.0, xs, xr, 10.0, zs, zr, v, 1e-3, nt, w, d)["datau"]
+    assert rel(out, ref) <= TOL_GATHER
+    assert ctx.status() == 0
