@@ -123,6 +123,24 @@ MNAD_API int mnad_fwd_fields(mnad_context* ctx, double dx, double xs, const doub
                              const double* w, int d_pml, int nkeep, const int* steps,
                              double* datau, double* fields);
 
+/* Forward modeling of one shot, as mnad_fwd_pde_exact(..., indx=0) with the
+ * default options, that allocates no device memory.  This entry point has no
+ * counterpart in the reference.  It is for callers that cannot let a library
+ * call cudaMalloc: applications whose GPU memory is already reserved by their
+ * own allocator, or processes that forbid allocation after start-up.  All of
+ * its working memory (wavefields, CPML memory variables, tables, the shot
+ * record) lives in one static device array of 64 MiB that every GPU loading
+ * the library holds until the process exits; a shot needing more (roughly a
+ * 1000 x 1000 padded grid, or a long record with many receivers) is rejected
+ * with MNAD_E_ARG.  The first call on a device sets up the array's device
+ * address on that device.  Calls share the array, clear it on entry and are
+ * serialised by the library; all pointers are host pointers, as in
+ * mnad_fwd_pde_exact.  No context is needed. */
+MNAD_API int mnad_fwd_pde_exact_noalloc(int device, double dx, double xs, const double* xr, int nr,
+                                        double dz, double zs, const double* zr,
+                                        const double* v, int nz, int nx, double dt, int nt,
+                                        const double* w, int d_pml, double* datau);
+
 /* Im = Born_adj_MNAD(dx,dz,nt,dt,v,xr,zr,data,d_pml,ss,Auu,...,Aww)
  * (SRC/migration/Born_adj_MNAD.m:1).  data is the nt x nr residual
  * (data{1} of the reference, :50); the source wavefield of shot `ss` must

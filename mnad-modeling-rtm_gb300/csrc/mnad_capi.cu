@@ -270,6 +270,26 @@ MNAD_API int mnad_fwd_fields(mnad_context* ctx, double dx, double xs, const doub
     });
 }
 
+MNAD_API int mnad_fwd_pde_exact_noalloc(int device, double dx, double xs, const double* xr, int nr,
+                                        double dz, double zs, const double* zr,
+                                        const double* v, int nz, int nx, double dt, int nt,
+                                        const double* w, int d_pml, double* datau)
+{
+    return guard([&] {
+        check_grid(nz, nx, d_pml, nt, dx, dz, dt, v);
+        need(w != nullptr, "w is NULL");
+        need(nr == 0 || datau != nullptr, "datau is NULL");
+        int n = 0;
+        MNAD_CK(cudaGetDeviceCount(&n));
+        need(device >= 0 && device < n, "no CUDA device " + std::to_string(device));
+        PropSpec s;
+        s.nz = nz; s.nx = nx;
+        fill_receivers(s, xr, zr, nr);
+        fwd_noalloc(device, dx, index1(xs, nx, "xs"), s.xr, dz, index1(zs, nz, "zs"), s.zr, v, nz, nx, dt, nt, w,
+                    d_pml, datau);
+    });
+}
+
 MNAD_API int mnad_born_adj(mnad_context* ctx, double dx, double dz, int nt, double dt,
                            const double* v, int nz, int nx, const double* xr, const double* zr, int nr,
                            const double* data, int d_pml, int ss, double* im)

@@ -174,7 +174,7 @@ int snapshot_T(int nt, int nf)
 
 // Stencil coefficient polynomials alpha*r + beta*r^2 (r = v^2 dt^2) of the
 // nine generator files (see the Coef enum for the centre entries).
-static void stencil_polys(double dx, double dz, float* al, float* be)
+void stencil_polys(double dx, double dz, float* al, float* be)
 {
     const double dx2 = dx * dx, dz2 = dz * dz, dx3 = dx2 * dx, dz3 = dz2 * dz;
     const double dx4 = dx2 * dx2, dz4 = dz2 * dz2, dx5 = dx4 * dx, dz5 = dz4 * dz;
@@ -218,7 +218,7 @@ static void stencil_polys(double dx, double dz, float* al, float* be)
     for (int k = 0; k < NCOEF; ++k) { al[k] = (float)a[k]; be[k] = (float)b[k]; }
 }
 
-static double r_of(double v, double dt, int mode)
+double r_of(double v, double dt, int mode)
 {
     return mode == MODE_ADJ ? (v * dt) * (v * dt) : (v * v) * (dt * dt);
 }

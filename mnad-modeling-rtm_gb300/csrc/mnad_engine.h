@@ -145,12 +145,25 @@ private:
     cudaGraphExec_t graph_ = nullptr;
 };
 
+// Stencil coefficient polynomials of one grid spacing (centre entries as in
+// the Coef enum) and r = v^2 dt^2 as the forward / adjoint compute it.
+void stencil_polys(double dx, double dz, float* al, float* be);
+double r_of(double v, double dt, int mode);
+
 // Model statistics for the reference's snapshot plan.
 void model_minmax(const double* v, size_t n, double& vmin, double& vmax);
 // nf of fwd_PDE_exact_MNAD.m:46 (may be 0).
 int snapshot_nf(int nt, double vmin, double vmax);
 // T of fwd_PDE_exact_MNAD.m:47 (throws when nf == 0).
 int snapshot_T(int nt, int nf);
+
+// Forward shot entirely inside the library's static scratch array (no device
+// allocation); indices 0-based.  Throws Error(MNAD_E_ARG) when the shot does
+// not fit.
+void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, double dz, int zs,
+                 const std::vector<int>& zr, const double* v, int nz, int nx, double dt, int nt, const double* w,
+                 int d, double* datau);
+size_t noalloc_scratch_bytes();
 
 // Device copies of the shot records (FP64, nt x nr).
 void upload(Context& ctx, void* dst, const void* src, size_t bytes);

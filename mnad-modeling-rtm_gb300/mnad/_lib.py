@@ -56,6 +56,8 @@ SIGNATURES = {
     "mnad_fwd_fields": ([_vp, C.c_double, C.c_double, _dp, C.c_int, C.c_double, C.c_double, _dp,
                          _dp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, C.c_int, C.c_int,
                          C.POINTER(C.c_int), _dp, _dp], C.c_int),
+    "mnad_fwd_pde_exact_noalloc": ([C.c_int, C.c_double, C.c_double, _dp, C.c_int, C.c_double, C.c_double, _dp,
+                                    _dp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, C.c_int, _dp], C.c_int),
     "mnad_born_adj": ([_vp, C.c_double, C.c_double, C.c_int, C.c_double, _dp, C.c_int, C.c_int, _dp, _dp,
                        C.c_int, _dp, C.c_int, C.c_int, _dp], C.c_int),
     "mnad_wavefield_info": ([_vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int), C.POINTER(C.c_int),
