@@ -92,6 +92,7 @@ struct __align__(16) PropDesc {
     double* dataw;
     // snapshots (forward with indx==1) / imaging (adjoint)
     int T;                   // 0: none
+    float invT;              // 1/T (exact quotients of tt/T via (tt + 0.5) * invT)
     int nsnap;               // snapshots filled by the forward: floor(nt/T)
     int ncols;               // columns of the reference's UU matrix
     int codec;

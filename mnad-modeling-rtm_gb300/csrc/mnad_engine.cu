@@ -323,6 +323,7 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     if (s.T > 0 && s.wf) {
         Wavefield& wf = *s.wf;
         D.T = s.T;
+        D.invT = 1.0f / (float)s.T;
         D.nsnap = wf.nsnap;
         D.ncols = wf.ncols;
         D.codec = wf.codec;
@@ -425,7 +426,9 @@ void Batch::finalize()
                     const bool interior = j0 >= d && j0 + TMA_TZ <= D.nz - d && i0 >= d && i0 + TMA_TX <= D.nx - d;
                     const int tl = tz + tx * D.ntz;
                     const int rb = p->tile_rec_host[tl], re = p->tile_rec_host[tl + 1];
-                    info.push_back(make_int4(rb, re, (interior ? 0 : TILE_STRIP) | (re > rb ? TILE_RECEIVERS : 0), tl));
+                    if (j0 >= (1 << 16) || i0 >= (1 << 15)) throw Error(MNAD_E_ARG, "grid too large for the TMA tiling");
+                    info.push_back(make_int4(rb, re, (interior ? 0 : TILE_STRIP) | (re > rb ? TILE_RECEIVERS : 0),
+                                             j0 | (i0 << 16)));
                 }
         }
         g->ntiles = (int)tile_prop.size();
@@ -466,7 +469,7 @@ void Batch::launch_step(int s)
         if (tc_.kind == MNAD_KERNEL_TMA) {
             const size_t smem = step_tma_smem_bytes();
             const int grid = std::min(g->ntiles, ctx_.num_sms * TMA_CTAS_PER_SM);
-            step_tma<<<grid, TMA_TZY * TMA_TX, smem, ctx_.stream>>>(a);
+            step_tma<<<grid, TMA_THREADS, smem, ctx_.stream>>>(a);
         } else
             step_direct<<<g->ntiles, dim3(DIRECT_TZ, DIRECT_TX), 0, ctx_.stream>>>(a);
     }

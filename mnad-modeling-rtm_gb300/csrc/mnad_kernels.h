@@ -9,18 +9,19 @@ namespace mnad {
 constexpr int DIRECT_TZ = 32;
 constexpr int DIRECT_TX = 8;
 
-// Tile of the TMA step kernel: TMA_TZY x TMA_TX threads, TMA_PZ consecutive
-// z points per thread.
-constexpr int TMA_TZY = 16;
-constexpr int TMA_TX = 16;
+// Tile of the TMA step kernel: TMA_TZ x TMA_TX points, TMA_TZY x TMA_TX
+// threads, TMA_PZ consecutive z points per thread.
 constexpr int TMA_PZ = 4;
-constexpr int TMA_TZ = TMA_TZY * TMA_PZ;
+constexpr int TMA_TZ = 64;
+constexpr int TMA_TX = 16;
+constexpr int TMA_TZY = TMA_TZ / TMA_PZ;
+constexpr int TMA_THREADS = TMA_TZY * TMA_TX;
 constexpr int TMA_STAGES = 3;         // tiles in flight per CTA
 constexpr int TMA_CTAS_PER_SM = 2;
 // Tensor maps of one propagation: halo boxes of U,V,W at both time levels,
 // point boxes of U,V,W at both levels, point box of r.
 constexpr int TMAP_HALO = 0, TMAP_POINT = 6, TMAP_R = 12, TMAPS_PER_PROP = 13;
-// tile_info.w flags
+// tile_info.z flags
 constexpr int TILE_STRIP = 1;         // intersects a CPML strip or the grid edge
 constexpr int TILE_RECEIVERS = 2;     // has receivers
 
