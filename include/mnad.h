@@ -75,6 +75,8 @@ typedef struct mnad_options {
                              them commented out, fwd_PDE_exact_MNAD.m:167-168) */
     int use_graphs;       /* capture the time loop in a CUDA graph (default 1) */
     int kernel;           /* MNAD_KERNEL_*; default AUTO */
+    int energy_every;     /* > 0: FP64 energy diagnostic of each forward every
+                             that many steps (read with mnad_context_energy) */
 } mnad_options;
 
 typedef struct mnad_context mnad_context;
@@ -93,6 +95,13 @@ MNAD_API int mnad_context_get_options(const mnad_context* ctx, mnad_options* opt
 MNAD_API int mnad_context_memory(const mnad_context* ctx, size_t* bytes_in_use);
 /* Host<->device bytes the context has copied so far (inputs, outputs). */
 MNAD_API int mnad_context_transfers(const mnad_context* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
+/* Energy history of the last forward run by mnad_fwd_pde_exact / mnad_fwd_fields
+ * with options.energy_every = K > 0: entry m (m = 0 .. floor(nt/K)-1) is, after
+ * step (m+1)K, E = 1/2 sum over the image region of ((U(t+1)-U(t))^2/(v dt)^2
+ * + V^2 + W^2) dx dz, accumulated in FP64 on the device (V = U_x, W = U_z are
+ * the MNAD gradient fields).  *n receives the number of entries; at most max
+ * are copied to out. */
+MNAD_API int mnad_context_energy(const mnad_context* ctx, double* out, int max, int* n);
 /* Bit set of device-side status flags seen so far (and clears them). */
 MNAD_API int mnad_context_status(mnad_context* ctx, unsigned* flags);
 
@@ -207,6 +216,13 @@ MNAD_API int mnad_plan_work(const mnad_plan* plan, double* point_updates, double
 /* Device time of the last run (ms, CUDA events on the plan's stream) and the
  * device time spent in step kernels only. */
 MNAD_API int mnad_plan_timing(const mnad_plan* plan, double* run_ms, double* step_ms, int* step_launches);
+/* Stack of the plan's RTM shots after mnad_plan_run, formed in FP64 on the
+ * device (SRC/migration/main_Acoustic_RTM.m:237-262): image_sum = sum of the
+ * shots' images (each T*sum US.*UR), illum_sum = sum of the shots'
+ * illuminations (each T*sum d2u^2), img_rtm = image_sum ./ illum_sum (the
+ * reference's mean(mhh,3)./illum; the 1/ns factors cancel).  All RTM jobs
+ * must share the grid.  Each output is Nint FP64 on the host, may be NULL. */
+MNAD_API int mnad_plan_stack(mnad_plan* plan, double* image_sum, double* illum_sum, double* img_rtm);
 
 #ifdef __cplusplus
 }

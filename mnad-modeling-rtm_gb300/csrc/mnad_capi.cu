@@ -88,10 +88,12 @@ MNAD_API int mnad_context_set_options(mnad_context* ctx, const mnad_options* o)
 {
     return guard([&] {
         need(ctx && o, "NULL argument");
-        need(o->snapshot_codec == MNAD_SNAP_F32 || o->snapshot_codec == MNAD_SNAP_BF16,
-             "snapshot_codec must be MNAD_SNAP_F32 or MNAD_SNAP_BF16");
+        need(o->snapshot_codec == MNAD_SNAP_F32 || o->snapshot_codec == MNAD_SNAP_BF16 ||
+                 o->snapshot_codec == MNAD_SNAP_F16,
+             "snapshot_codec must be MNAD_SNAP_F32, MNAD_SNAP_BF16 or MNAD_SNAP_F16");
         need(o->pairing == MNAD_PAIR_REFERENCE || o->pairing == MNAD_PAIR_ALIGNED, "bad pairing");
         need(o->kernel >= MNAD_KERNEL_AUTO && o->kernel <= MNAD_KERNEL_TMA, "bad kernel");
+        need(o->energy_every >= 0, "energy_every must be >= 0");
         ctx->opt = *o;
     });
 }
@@ -121,6 +123,17 @@ MNAD_API int mnad_context_transfers(const mnad_context* ctx, uint64_t* h2d, uint
     });
 }
 
+MNAD_API int mnad_context_energy(const mnad_context* ctx, double* out, int max, int* n)
+{
+    return guard([&] {
+        need(ctx != nullptr, "context is NULL");
+        const int m = (int)ctx->last_energy.size();
+        if (n) *n = m;
+        if (out)
+            for (int k = 0; k < std::min(m, max); ++k) out[k] = ctx->last_energy[k];
+    });
+}
+
 MNAD_API int mnad_context_status(mnad_context* ctx, unsigned* flags)
 {
     return guard([&] {
@@ -146,6 +159,9 @@ static std::unique_ptr<Wavefield> new_wavefield(Context& c, int nz, int nx, int 
         wf->scale = DevMem(&c, std::max(1, nsnap) * sizeof(float));
         std::vector<float> one(std::max(1, nsnap), 1.0f);
         upload(c, wf->scale.get(), one.data(), one.size() * sizeof(float));
+        wf->stage = DevMem(&c, std::max<size_t>(1, wf->nint * sizeof(float)));
+        wf->maxbits = DevMem(&c, std::max(1, nsnap) * sizeof(unsigned));
+        MNAD_CK(cudaMemsetAsync(wf->maxbits.get(), 0, wf->maxbits.size(), c.stream));
     }
     return wf;
 }
@@ -184,6 +200,7 @@ MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const d
         s.xs = index1(xs, nx, "xs");
         fill_receivers(s, xr, zr, nr);
         s.record_vw = c.opt.record_vw && (datav || dataw);
+        s.energy_every = c.opt.energy_every;
         std::unique_ptr<Wavefield> wf;
         if (indx == 1) {
             double vmin, vmax;
@@ -207,6 +224,8 @@ MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const d
         download(c, datau, p.data.get(), nd * sizeof(double));
         if (s.record_vw && datav) download(c, datav, p.datav.get(), nd * sizeof(double));
         if (s.record_vw && dataw) download(c, dataw, p.dataw.get(), nd * sizeof(double));
+        c.last_energy.assign(p.energy.size() / sizeof(double), 0.0);
+        if (!c.last_energy.empty()) download(c, c.last_energy.data(), p.energy.get(), p.energy.size());
         c.sync();
         if (wf) c.wavefields[ss] = std::move(wf);
     });
@@ -236,6 +255,7 @@ MNAD_API int mnad_fwd_fields(mnad_context* ctx, double dx, double xs, const doub
         s.zs = index1(zs, nz, "zs");
         s.xs = index1(xs, nx, "xs");
         fill_receivers(s, xr, zr, nr);
+        s.energy_every = c.opt.energy_every;
         Prop p;
         p.spec = s;
         const TileCfg tc = tile_cfg(c.opt.kernel);
@@ -266,6 +286,8 @@ MNAD_API int mnad_fwd_fields(mnad_context* ctx, double dx, double xs, const doub
         }
         b.advance(done, nt);
         download(c, datau, p.data.get(), (size_t)nt * nr * sizeof(double));
+        c.last_energy.assign(p.energy.size() / sizeof(double), 0.0);
+        if (!c.last_energy.empty()) download(c, c.last_energy.data(), p.energy.get(), p.energy.size());
         c.sync();
     });
 }
@@ -397,6 +419,20 @@ MNAD_API int mnad_wavefield_import(mnad_context* ctx, int ss, int nz, int nx, in
         MNAD_CK(cudaSetDevice(c.device));
         auto wf = new_wavefield(c, nz, nx, d_pml, nt, T, ncols, nsnap, c.opt.snapshot_codec);
         const size_t n = wf->nint * (size_t)nsnap;
+        if (wf->codec == MNAD_SNAP_F16 && nsnap > 0) {
+            // per-column power-of-two scales, as the forward's encoder picks them
+            std::vector<float> sc(nsnap, 1.0f);
+            for (int k = 0; k < nsnap; ++k) {
+                double mx = 0;
+                for (size_t q = 0; q < wf->nint; ++q) mx = std::max(mx, std::fabs(UU[(size_t)k * wf->nint + q]));
+                if (mx > 0) {
+                    int e = 0;
+                    std::frexp((float)mx, &e);
+                    sc[k] = std::ldexp(1.0f, e - 14);
+                }
+            }
+            upload(c, wf->scale.get(), sc.data(), sc.size() * sizeof(float));
+        }
         if (n) {
             DevMem tmp(&c, n * sizeof(double));
             upload(c, tmp.get(), UU, n * sizeof(double));
@@ -626,6 +662,40 @@ MNAD_API int mnad_plan_timing(const mnad_plan* P, double* run_ms, double* step_m
         if (run_ms) *run_ms = P->run_ms;
         if (step_ms) *step_ms = P->step_ms;
         if (launches) *launches = P->launches;
+    });
+}
+
+MNAD_API int mnad_plan_stack(mnad_plan* P, double* image_sum, double* illum_sum, double* img_rtm)
+{
+    return guard([&] {
+        need(P != nullptr, "plan is NULL");
+        Context& c = *P->ctx;
+        MNAD_CK(cudaSetDevice(c.device));
+        Prop* first = nullptr;
+        for (Prop* a : P->adj)
+            if (a) {
+                if (!first) first = a;
+                need(a->nint() == first->nint() && a->spec.nz == first->spec.nz && a->spec.nx == first->spec.nx,
+                     "mnad_plan_stack: RTM jobs have different grids");
+            }
+        need(first != nullptr, "mnad_plan_stack: the plan has no RTM job");
+        const size_t n = first->nint();
+        const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+        DevMem im(&c, n * sizeof(double)), il(&c, n * sizeof(double)), out(&c, n * sizeof(double));
+        MNAD_CK(cudaMemsetAsync(im.get(), 0, im.size(), c.stream));
+        MNAD_CK(cudaMemsetAsync(il.get(), 0, il.size(), c.stream));
+        for (Prop* a : P->adj) {
+            if (!a) continue;
+            const double T = (double)a->spec.T;
+            axpy_f64<<<blocks, 256, 0, c.stream>>>(T, a->image.as<double>(), n, im.as<double>());
+            axpy_f64<<<blocks, 256, 0, c.stream>>>(T, a->spec.wf->illum.as<double>(), n, il.as<double>());
+        }
+        divide_f64<<<blocks, 256, 0, c.stream>>>(im.as<double>(), il.as<double>(), n, out.as<double>());
+        MNAD_CK(cudaGetLastError());
+        if (image_sum) download(c, image_sum, im.get(), n * sizeof(double));
+        if (illum_sum) download(c, illum_sum, il.get(), n * sizeof(double));
+        if (img_rtm) download(c, img_rtm, out.get(), n * sizeof(double));
+        c.sync();
     });
 }
 

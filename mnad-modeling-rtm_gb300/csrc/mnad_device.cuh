@@ -99,6 +99,8 @@ struct __align__(16) PropDesc {
     int pairing;
     int img_steps;           // adjoint: number of imaging steps floor(nt/T)
     void* snap;              // [ncols' = nsnap][nint]
+    int snap_stage;          // forward with the FP16 codec: every snapshot is
+                             // written in FP32 to one staging slot, then encoded
     const float* snap_scale; // per-snapshot scale (FP16 codec), may be null
     double* illum;           // [nint] sum of d2u^2 (forward)
     double* image;           // [nint] sum of US.*UR (adjoint)

@@ -61,6 +61,7 @@ Context::Context(int dev, size_t budget_bytes) : device(dev), budget(budget_byte
     opt.record_vw = 0;
     opt.use_graphs = 1;
     opt.kernel = MNAD_KERNEL_AUTO;
+    opt.energy_every = 0;
 }
 
 Context::~Context()
@@ -320,6 +321,8 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     D.rec_pt = rec_pt.as<int>(); D.rec_id = rec_id.as<int>(); D.rec_r = rec_r.as<double>();
     D.data = data.as<double>(); D.datav = datav.as<double>(); D.dataw = dataw.as<double>();
 
+    if (s.mode == MODE_FWD && s.energy_every > 0 && s.nt / s.energy_every > 0)
+        energy = DevMem(&ctx, (size_t)(s.nt / s.energy_every) * sizeof(double));
     if (s.T > 0 && s.wf) {
         Wavefield& wf = *s.wf;
         D.T = s.T;
@@ -330,6 +333,11 @@ void Prop::build(Context& ctx, const TileCfg& tc)
         D.pairing = s.pairing;
         D.snap = wf.snap.get();
         D.snap_scale = wf.scale.as<float>();
+        if (s.mode == MODE_FWD && wf.codec == MNAD_SNAP_F16) {
+            D.snap = wf.stage.get();        // FP32 staging slot, encoded after each snapshot step
+            D.codec = CODEC_F32;
+            D.snap_stage = 1;
+        }
         if (s.mode == MODE_FWD) {
             D.illum = wf.illum.as<double>();
         } else {
@@ -349,9 +357,12 @@ void Prop::reset(Context& ctx)
     if (spec.mode == MODE_FWD) {
         if (data.get()) MNAD_CK(cudaMemsetAsync(data.get(), 0, data.size(), st));
         if (desc.illum) MNAD_CK(cudaMemsetAsync(desc.illum, 0, nint() * sizeof(double), st));
+        if (spec.wf && spec.wf->maxbits.get())
+            MNAD_CK(cudaMemsetAsync(spec.wf->maxbits.get(), 0, spec.wf->maxbits.size(), st));
     } else if (image.get()) {
         MNAD_CK(cudaMemsetAsync(image.get(), 0, image.size(), st));
     }
+    if (energy.get()) MNAD_CK(cudaMemsetAsync(energy.get(), 0, energy.size(), st));
 }
 
 double Prop::algorithmic_bytes() const
@@ -446,6 +457,11 @@ void Batch::finalize()
     }
     if (tc_.kind == MNAD_KERNEL_TMA)
         d_counters_ = DevMem(&ctx_, std::max<size_t>(1, (size_t)nsteps_ * groups_.size()) * sizeof(int));
+    for (Prop* p : props_)
+        if (p->energy.get()) {
+            p->d_desc = DevMem(&ctx_, sizeof(PropDesc));
+            upload(ctx_, p->d_desc.get(), &p->desc, sizeof(PropDesc));
+        }
     d_all_desc_ = DevMem(&ctx_, std::max<size_t>(1, all.size()) * sizeof(PropDesc));
     upload(ctx_, d_all_desc_.get(), all.data(), all.size() * sizeof(PropDesc));
 }
@@ -485,10 +501,49 @@ void Batch::start()
     MNAD_CK(cudaGetLastError());
 }
 
+void Batch::encode_snapshots(int s)
+{
+    for (Prop* p : props_) {
+        const PropSpec& sp = p->spec;
+        if (sp.mode != MODE_FWD || !sp.wf || sp.wf->codec != MNAD_SNAP_F16 || sp.T <= 0) continue;
+        const int tt = s + 1;
+        if (tt > sp.nt || tt % sp.T != 0 || tt / sp.T > sp.wf->nsnap) continue;
+        const int k = tt / sp.T - 1;
+        Wavefield& wf = *sp.wf;
+        const size_t n = wf.nint;
+        const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)ctx_.num_sms * 4);
+        f16_absmax<<<blocks, 256, 0, ctx_.stream>>>(wf.stage.as<float>(), n, wf.maxbits.as<unsigned>() + k);
+        f16_encode<<<blocks, 256, 0, ctx_.stream>>>(wf.stage.as<float>(), n, wf.maxbits.as<unsigned>() + k,
+                                                    wf.snap.as<__half>() + (size_t)k * n, wf.scale.as<float>() + k);
+    }
+}
+
+void Batch::energy_after(int s)
+{
+    for (Prop* p : props_) {
+        const int K = p->spec.energy_every;
+        if (!p->energy.get() || (s + 1) % K != 0 || s + 1 > p->spec.nt) continue;
+        const size_t n = p->nint();
+        const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)ctx_.num_sms * 2);
+        // after step s the new fields are time level (s + 1) & 1
+        energy_reduce<<<std::max(blocks, 1), 256, 0, ctx_.stream>>>(p->d_desc.as<PropDesc>(), (s + 1) & 1,
+                                                                    p->energy.as<double>() + (s + 1) / K - 1);
+    }
+}
+
 void Batch::advance(int s0, int s1)
 {
     if (ntiles_ == 0) return;
-    for (int s = s0; s < s1; ++s) launch_step(s);
+    bool f16 = false, en = false;
+    for (Prop* p : props_) {
+        f16 |= p->spec.mode == MODE_FWD && p->spec.wf && p->spec.wf->codec == MNAD_SNAP_F16;
+        en |= p->energy.get() != nullptr;
+    }
+    for (int s = s0; s < s1; ++s) {
+        launch_step(s);
+        if (f16) encode_snapshots(s);
+        if (en) energy_after(s);
+    }
     MNAD_CK(cudaGetLastError());
 }
 

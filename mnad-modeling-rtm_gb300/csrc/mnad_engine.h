@@ -51,6 +51,7 @@ struct Wavefield {
     int nz = 0, nx = 0, d = 0, nt = 0, T = 0, nsnap = 0, ncols = 0, codec = 0;
     size_t nint = 0;
     DevMem snap, scale, illum;
+    DevMem stage, maxbits;   // FP16 codec: FP32 staging snapshot, per-snapshot max |d2u|
 };
 
 struct Context {
@@ -63,6 +64,7 @@ struct Context {
     int num_sms = 0;
     unsigned* d_status = nullptr;
     std::map<int, std::unique_ptr<Wavefield>> wavefields;
+    std::vector<double> last_energy;  // energy history of the last drop-in forward
 
     explicit Context(int dev, size_t budget_bytes);
     ~Context();
@@ -92,6 +94,7 @@ struct PropSpec {
     Wavefield* wf = nullptr;           // forward: snapshots to fill; adjoint: to image with
     int T = 0;                         // snapshot / imaging interval (0: none)
     int pairing = MNAD_PAIR_REFERENCE;
+    int energy_every = 0;              // forward: FP64 energy every that many steps
 };
 
 // Device state of one propagation.
@@ -102,6 +105,7 @@ struct Prop {
     size_t S = 0;                      // floats per field in storage
     std::vector<int> tile_rec_host;    // receiver bucket offsets per tile
     DevMem fields, r, mx, mz, src_amp, rec_pt, rec_id, rec_r, tile_rec, data, datav, dataw, image;
+    DevMem energy, d_desc;             // energy history; this propagation's descriptor on the device
     void build(Context& ctx, const TileCfg& tc);
     void reset(Context& ctx);          // zero the state of a fresh run (stream-ordered)
     size_t nint() const { return (size_t)(spec.nz - 2 * spec.d) * (spec.nx - 2 * spec.d); }
@@ -135,6 +139,8 @@ public:
     const std::vector<Prop*>& props() const { return props_; }
 private:
     void launch_step(int s);
+    void encode_snapshots(int s);      // FP16 codec: encode the snapshots taken at step s
+    void energy_after(int s);          // energy diagnostic after step s
     Context& ctx_;
     TileCfg tc_;
     std::vector<Prop*> props_;

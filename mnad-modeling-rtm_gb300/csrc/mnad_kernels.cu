@@ -143,6 +143,71 @@ __global__ void scale_f64(const double* __restrict__ in, double s, size_t n, dou
 
 namespace mnad {
 
+// Largest |x| of one FP32 snapshot (positive floats order like their bits).
+__global__ void f16_absmax(const float* __restrict__ x, size_t n, unsigned* __restrict__ maxbits)
+{
+    float m = 0.0f;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(x[k]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(maxbits, __float_as_uint(m));
+}
+
+// FP16 encoding of one snapshot with a power-of-two scale s chosen from its
+// maximum so that max/s < 2^14 (no saturation; the scale multiply is exact).
+__global__ void f16_encode(const float* __restrict__ x, size_t n, const unsigned* __restrict__ maxbits,
+                           __half* __restrict__ out, float* __restrict__ scale)
+{
+    const float mx = __uint_as_float(*maxbits);
+    int e = 0;
+    frexpf(mx, &e);                                   // mx = f * 2^e, 0.5 <= f < 1
+    const float s = mx > 0.0f ? ldexpf(1.0f, e - 14) : 1.0f;
+    const float inv = mx > 0.0f ? ldexpf(1.0f, 14 - e) : 1.0f;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *scale = s;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        out[k] = __float2half_rn(x[k] * inv);
+}
+
+// Energy of one propagation after a step, in FP64 over the image region:
+// 1/2 sum ((Unew - Uold)^2 / r + Vnew^2 + Wnew^2) * dx * dz.
+__global__ void energy_reduce(const PropDesc* __restrict__ desc, int lvl_new, double* __restrict__ out)
+{
+    const PropDesc& P = *desc;
+    const int d = P.d, niz = P.nz - 2 * d, nix = P.nx - 2 * d;
+    const size_t n = (size_t)niz * nix;
+    const float* Un = P.fld[lvl_new][0];
+    const float* Uo = P.fld[lvl_new ^ 1][0];
+    const float* Vn = P.fld[lvl_new][1];
+    const float* Wn = P.fld[lvl_new][2];
+    double acc = 0.0;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(k % niz) + d, i = (int)(k / niz) + d;
+        const size_t o = (size_t)(i + HX) * P.ld + (j + HZ);
+        const double du = (double)Un[o] - (double)Uo[o];
+        const double v = Vn[o], w = Wn[o];
+        acc += du * du / (double)P.r[o] + v * v + w * w;
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, 0.5 * (double)P.dx * (double)P.dz * acc);
+}
+
+// y += a * x in FP64 (the image / illumination stack over shots,
+// main_Acoustic_RTM.m:237-244,256-262).
+__global__ void axpy_f64(double a, const double* __restrict__ x, size_t n, double* __restrict__ y)
+{
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        y[k] = fma(a, x[k], y[k]);
+}
+
+// out = num ./ den with IEEE semantics (img_RTM = mean(mhh,3)./illum,
+// main_Acoustic_RTM.m:262; a zero illumination gives Inf/NaN as in MATLAB).
+__global__ void divide_f64(const double* __restrict__ num, const double* __restrict__ den, size_t n,
+                           double* __restrict__ out)
+{
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        out[k] = num[k] / den[k];
+}
+
 // Scattered data of the RTM workflow: data_sct = data - datas
 // (main_Acoustic_RTM.m:225), formed on the device.
 __global__ void residual_f64(const double* __restrict__ a, const double* __restrict__ b, size_t n,

@@ -38,6 +38,13 @@ __global__ void snap_import(const double* __restrict__ in, int codec, const floa
 __global__ void field_export(const float* __restrict__ F, int nz, int nx, int ld, int fix_at, float fix,
                              double* __restrict__ out);
 __global__ void scale_f64(const double* __restrict__ in, double s, size_t n, double* __restrict__ out);
+__global__ void f16_absmax(const float* __restrict__ x, size_t n, unsigned* __restrict__ maxbits);
+__global__ void f16_encode(const float* __restrict__ x, size_t n, const unsigned* __restrict__ maxbits,
+                           __half* __restrict__ out, float* __restrict__ scale);
+__global__ void energy_reduce(const PropDesc* __restrict__ desc, int lvl_new, double* __restrict__ out);
+__global__ void axpy_f64(double a, const double* __restrict__ x, size_t n, double* __restrict__ y);
+__global__ void divide_f64(const double* __restrict__ num, const double* __restrict__ den, size_t n,
+                           double* __restrict__ out);
 __global__ void residual_f64(const double* __restrict__ a, const double* __restrict__ b, size_t n,
                              double* __restrict__ out);
 

@@ -127,13 +127,9 @@ __device__ __forceinline__ void finish_point(const PropDesc& P, int tt, int j, i
             d2u *= P.inv_dt2;
             const size_t q = (size_t)(j - d) + (size_t)(i - d) * niz;
             const size_t nint = (size_t)niz * (P.nx - 2 * d);
-            const size_t o = (size_t)(tt / P.T - 1) * nint + q;
+            const size_t o = (P.snap_stage ? (size_t)0 : (size_t)(tt / P.T - 1)) * nint + q;
             if (P.codec == CODEC_BF16) static_cast<__nv_bfloat16*>(P.snap)[o] = __float2bfloat16_rn(d2u);
-            else if (P.codec == CODEC_F16) {
-                const float e = d2u * (1.0f / P.snap_scale[tt / P.T - 1]);   // power of two: exact
-                if (!(fabsf(e) <= 65504.0f)) atomicOr(P.status, ST_F16_RANGE);
-                static_cast<__half*>(P.snap)[o] = __float2half_rn(e);
-            } else static_cast<float*>(P.snap)[o] = d2u;
+            else static_cast<float*>(P.snap)[o] = d2u;   // FP32, or the FP16 codec's staging slot
             P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
         }
         if ((long long)p == P.src && tt < P.nt) xu += P.src_amp[tt];   // next step's injection

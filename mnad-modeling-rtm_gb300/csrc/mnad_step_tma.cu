@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                         else if (tt == 2) d2u = su[k] - pu[k];
                         d2u *= P.inv_dt2;
                         const size_t q = (size_t)(q0 + k);
-                        const size_t o = (size_t)(tq - 1) * nint + q;
+                        const size_t o = (P.snap_stage ? (size_t)0 : (size_t)(tq - 1)) * nint + q;
                         if (P.codec == CODEC_BF16) static_cast<__nv_bfloat16*>(P.snap)[o] = __float2bfloat16_rn(d2u);
                         else static_cast<float*>(P.snap)[o] = d2u;
                         P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
@@ -561,7 +561,8 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                     if (adj_inj) xu -= injection(P, tt, rbeg, rend, p + k);
                     if (col && inner) {
                         const size_t q = (size_t)(q0 + k);
-                        const float us = snap_decode(P.snap, P.codec, (size_t)(col - 1) * nint + q, 1.0f);
+                        const float sc = P.codec == CODEC_F16 ? P.snap_scale[col - 1] : 1.0f;
+                        const float us = snap_decode(P.snap, P.codec, (size_t)(col - 1) * nint + q, sc);
                         P.image[q] = fma((double)us, (double)xu, P.image[q]);
                     }
                 }

@@ -29,7 +29,8 @@ _vp = C.c_void_p
 
 class Options(C.Structure):
     _fields_ = [("snapshot_codec", C.c_int), ("pairing", C.c_int), ("T", C.c_int),
-                ("record_vw", C.c_int), ("use_graphs", C.c_int), ("kernel", C.c_int)]
+                ("record_vw", C.c_int), ("use_graphs", C.c_int), ("kernel", C.c_int),
+                ("energy_every", C.c_int)]
 
 
 class Job(C.Structure):
@@ -49,6 +50,7 @@ SIGNATURES = {
     "mnad_context_get_options": ([_vp, C.POINTER(Options)], C.c_int),
     "mnad_context_memory": ([_vp, C.POINTER(C.c_size_t)], C.c_int),
     "mnad_context_status": ([_vp, C.POINTER(C.c_uint)], C.c_int),
+    "mnad_context_energy": ([_vp, _dp, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "mnad_context_transfers": ([_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], C.c_int),
     "mnad_fwd_pde_exact": ([_vp, C.c_double, C.c_double, _dp, C.c_int, C.c_double, C.c_double, _dp,
                             _dp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, C.c_int, C.c_int, C.c_int,
@@ -73,6 +75,7 @@ SIGNATURES = {
     "mnad_plan_destroy": ([_vp], C.c_int),
     "mnad_plan_work": ([_vp, _dp, _dp], C.c_int),
     "mnad_plan_timing": ([_vp, _dp, _dp, C.POINTER(C.c_int)], C.c_int),
+    "mnad_plan_stack": ([_vp, _dp, _dp, _dp], C.c_int),
 }
 
 

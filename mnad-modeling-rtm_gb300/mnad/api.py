@@ -72,10 +72,10 @@ class Context:
         inv = lambda d, v: next(k for k, x in d.items() if x == v)
         return {"snapshot_codec": inv(_CODECS, o.snapshot_codec), "pairing": inv(_PAIRINGS, o.pairing),
                 "T": o.T, "record_vw": bool(o.record_vw), "use_graphs": bool(o.use_graphs),
-                "kernel": inv(_KERNELS, o.kernel)}
+                "kernel": inv(_KERNELS, o.kernel), "energy_every": o.energy_every}
 
     def set_options(self, snapshot_codec=None, pairing=None, T=None, record_vw=None, use_graphs=None,
-                    kernel=None):
+                    kernel=None, energy_every=None):
         o = Options()
         check(lib().mnad_context_get_options(self._h, C.byref(o)))
         if snapshot_codec is not None:
@@ -90,6 +90,8 @@ class Context:
             o.use_graphs = int(bool(use_graphs))
         if kernel is not None:
             o.kernel = _KERNELS[kernel]
+        if energy_every is not None:
+            o.energy_every = int(energy_every)
         check(lib().mnad_context_set_options(self._h, C.byref(o)))
 
     def memory(self) -> int:
@@ -102,6 +104,14 @@ class Context:
         a, b = C.c_uint64(), C.c_uint64()
         check(lib().mnad_context_transfers(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def energy(self) -> np.ndarray:
+        """Energy history of the last forward (see mnad_context_energy)."""
+        n = C.c_int()
+        check(lib().mnad_context_energy(self._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        check(lib().mnad_context_energy(self._h, _ptr(out), n.value, C.byref(n)))
+        return out
 
     def status(self) -> int:
         f = C.c_uint()
@@ -292,6 +302,16 @@ class Plan:
         r, s, n = C.c_double(), C.c_double(), C.c_int()
         check(lib().mnad_plan_timing(self._h, C.byref(r), C.byref(s), C.byref(n)))
         return {"run_ms": r.value, "step_ms": s.value, "step_launches": n.value}
+
+    def stack(self):
+        """(image_sum, illum_sum, img_rtm) of the RTM shots, (nz-2d, nx-2d) arrays."""
+        rtm = [j for j in self.jobs if j.kind == "rtm"]
+        if not rtm:
+            raise MnadError(_lib.E_ARG, "the plan has no RTM job")
+        shape = rtm[0].image.shape
+        outs = [np.zeros(shape, order="F") for _ in range(3)]
+        check(lib().mnad_plan_stack(self._h, *[_ptr(o) for o in outs]))
+        return tuple(outs)
 
     def close(self):
         if getattr(self, "_h", None):
