@@ -1,5 +1,6 @@
 // C ABI of libmnad.so (declared in include/mnad.h).
 #include "mnad_engine.h"
+#include "mnad_jobs.h"
 #include "mnad_kernels.h"
 
 #include <algorithm>
@@ -13,59 +14,13 @@ struct mnad_context : Context {
     using Context::Context;
 };
 
-static thread_local std::string g_err;
-
-template <class F>
-static int guard(F&& f)
-{
-    try {
-        f();
-        return MNAD_OK;
-    } catch (const Error& e) {
-        g_err = e.what();
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        g_err = "host allocation failed";
-        return MNAD_E_OOM;
-    } catch (const std::exception& e) {
-        g_err = e.what();
-        return MNAD_E_CUDA;
-    }
-}
-
-static void need(bool ok, const std::string& msg)
-{
-    if (!ok) throw Error(MNAD_E_ARG, msg);
-}
-
-// 1-based grid index passed as a double (MATLAB) -> 0-based int.
-static int index1(double x, int n, const char* what)
-{
-    need(std::isfinite(x) && x == std::floor(x) && x >= 1 && x <= n,
-         std::string(what) + " must be an integer grid index in [1, " + std::to_string(n) + "], got " + std::to_string(x));
-    return (int)x - 1;
-}
-
-static void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, const double* v)
-{
-    need(v != nullptr, "v is NULL");
-    need(nz >= 1 && nx >= 1, "grid must be at least 1 x 1");
-    need(d >= 0 && nz >= 2 * d && nx >= 2 * d, "d_pml must satisfy 0 <= 2*d_pml <= min(nz, nx) (C_cof.m builds the strips)");
-    need(nt >= 1, "nt must be >= 1");
-    need(std::isfinite(dx) && dx > 0 && std::isfinite(dz) && dz > 0 && std::isfinite(dt) && dt > 0,
-         "dx, dz, dt must be positive and finite");
-    const size_t n = (size_t)nz * nx;
-    for (size_t k = 0; k < n; ++k)
-        need(std::isfinite(v[k]) && v[k] > 0, "velocity must be positive and finite (entry " + std::to_string(k) + ")");
-}
-
 static bool use_graph(const Context& c, int nt) { return c.opt.use_graphs != 0 && nt >= 1; }
 
 extern "C" {
 
 MNAD_API int mnad_abi_version(void) { return MNAD_ABI_VERSION; }
 
-MNAD_API const char* mnad_last_error(void) { return g_err.c_str(); }
+MNAD_API const char* mnad_last_error(void) { return last_error().c_str(); }
 
 MNAD_API int mnad_context_create(int device, size_t hbm_budget_bytes, mnad_context** out)
 {
@@ -144,40 +99,6 @@ MNAD_API int mnad_context_status(mnad_context* ctx, unsigned* flags)
 }
 
 // ---------------------------------------------------------------------------
-static std::unique_ptr<Wavefield> new_wavefield(Context& c, int nz, int nx, int d, int nt, int T, int ncols,
-                                                int nsnap, int codec)
-{
-    auto wf = std::make_unique<Wavefield>();
-    wf->nz = nz; wf->nx = nx; wf->d = d; wf->nt = nt; wf->T = T;
-    wf->ncols = ncols; wf->nsnap = nsnap; wf->codec = codec;
-    wf->nint = (size_t)(nz - 2 * d) * (nx - 2 * d);
-    const size_t cb = codec == MNAD_SNAP_F32 ? 4 : 2;
-    wf->snap = DevMem(&c, std::max<size_t>(1, wf->nint * (size_t)nsnap * cb));
-    wf->illum = DevMem(&c, std::max<size_t>(1, wf->nint * sizeof(double)));
-    MNAD_CK(cudaMemsetAsync(wf->illum.get(), 0, wf->illum.size(), c.stream));
-    if (codec == MNAD_SNAP_F16) {
-        wf->scale = DevMem(&c, std::max(1, nsnap) * sizeof(float));
-        std::vector<float> one(std::max(1, nsnap), 1.0f);
-        upload(c, wf->scale.get(), one.data(), one.size() * sizeof(float));
-        wf->stage = DevMem(&c, std::max<size_t>(1, wf->nint * sizeof(float)));
-        wf->maxbits = DevMem(&c, std::max(1, nsnap) * sizeof(unsigned));
-        MNAD_CK(cudaMemsetAsync(wf->maxbits.get(), 0, wf->maxbits.size(), c.stream));
-    }
-    return wf;
-}
-
-static void fill_receivers(PropSpec& s, const double* xr, const double* zr, int nr)
-{
-    need(nr >= 0, "nr must be >= 0");
-    need(nr == 0 || (xr && zr), "receiver index arrays are NULL");
-    s.zr.resize(nr);
-    s.xr.resize(nr);
-    for (int k = 0; k < nr; ++k) {
-        s.zr[k] = index1(zr[k], s.nz, "zr");
-        s.xr[k] = index1(xr[k], s.nx, "xr");
-    }
-}
-
 MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const double* xr, int nr,
                                 double dz, double zs, const double* zr,
                                 const double* v, int nz, int nx, double dt, int nt,
@@ -488,35 +409,10 @@ struct mnad_plan {
     }
 };
 
-static void check_job(const mnad_job& j, int k)
-{
-    const std::string pre = "job " + std::to_string(k) + ": ";
-    need(j.kind == MNAD_JOB_MODEL || j.kind == MNAD_JOB_RTM, pre + "kind must be MNAD_JOB_MODEL or MNAD_JOB_RTM");
-    check_grid(j.nz, j.nx, j.d_pml, j.nt, j.dx, j.dz, j.dt, j.v);
-    need(j.w != nullptr, pre + "w is NULL");
-    if (j.kind == MNAD_JOB_RTM) {
-        check_grid(j.nz, j.nx, j.d_pml, j.nt, j.dx, j.dz, j.dt, j.vs);
-        need(j.image_out != nullptr, pre + "image_out is NULL");
-    } else {
-        need(j.nr == 0 || j.data_out != nullptr, pre + "data_out is NULL");
-    }
-}
-
 static Prop* add_prop(mnad_plan& P, const mnad_job& j, int mode, const double* v, Wavefield* wf, int T)
 {
     auto p = std::make_unique<Prop>();
-    PropSpec& s = p->spec;
-    s.mode = mode;
-    s.nz = j.nz; s.nx = j.nx; s.d = j.d_pml; s.nt = j.nt;
-    s.dx = j.dx; s.dz = j.dz; s.dt = j.dt; s.v = v; s.w = j.w;
-    if (mode == MODE_FWD) {
-        s.zs = index1(j.zs, j.nz, "zs");
-        s.xs = index1(j.xs, j.nx, "xs");
-    }
-    fill_receivers(s, j.xr, j.zr, j.nr);
-    s.wf = wf;
-    s.T = T;
-    s.pairing = P.ctx->opt.pairing;
+    p->spec = job_spec(j, mode, v, wf, T, P.ctx->opt.pairing);
     P.props.push_back(std::move(p));
     return P.props.back().get();
 }
@@ -545,13 +441,9 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
             const mnad_job& j = jobs[k];
             P->fwd_true[k] = add_prop(*P, j, MODE_FWD, j.v, nullptr, 0);
             if (j.kind == MNAD_JOB_RTM) {
-                double vmin, vmax;
-                model_minmax(j.vs, (size_t)j.nz * j.nx, vmin, vmax);
-                const int nf = snapshot_nf(j.nt, vmin, vmax);
-                const int T = j.T > 0 ? j.T : snapshot_T(j.nt, nf);
-                const int ks = j.nt / T;
-                P->wfs.push_back(new_wavefield(c, j.nz, j.nx, j.d_pml, j.nt, T, std::max(2 * nf + 1, ks), ks,
-                                               c.opt.snapshot_codec));
+                int T, ncols;
+                rtm_snapshot_plan(j, T, ncols);
+                P->wfs.push_back(new_wavefield(c, j.nz, j.nx, j.d_pml, j.nt, T, ncols, j.nt / T, c.opt.snapshot_codec));
                 Wavefield* wf = P->wfs.back().get();
                 P->fwd_bg[k] = add_prop(*P, j, MODE_FWD, j.vs, wf, T);
                 P->adj[k] = add_prop(*P, j, MODE_ADJ, j.vs, wf, T);
@@ -706,10 +598,10 @@ MNAD_API int mnad_run_jobs(mnad_context* ctx, const mnad_job* jobs, int njobs)
     if (rc != MNAD_OK) return rc;
     rc = mnad_plan_run(P);
     if (rc == MNAD_OK) rc = mnad_plan_download(P);
-    const std::string keep = g_err;
+    const std::string keep = last_error();
     const int rc2 = mnad_plan_destroy(P);
     if (rc != MNAD_OK) {
-        g_err = keep;
+        last_error() = keep;
         return rc;
     }
     return rc2;

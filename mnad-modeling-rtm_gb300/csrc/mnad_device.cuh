@@ -69,6 +69,7 @@ struct __align__(16) PropDesc {
     int dpz;           // pitch of one z-strip column (floats, >= d + 6, multiple of 4)
     int zb0;           // first storage row of the bottom z strip: (nz - d) rounded down to 4
     int tile_base;     // first global tile of this propagation
+    int s_off;         // global step at which this propagation started (even)
     int ntz, ntx;      // tiles along z / x
     float* fld[2][3];  // [time level][U,V,W], storage origin (halo included)
     const float* r;    // v^2 dt^2, same storage

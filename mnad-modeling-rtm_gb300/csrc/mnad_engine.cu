@@ -321,6 +321,7 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     D.rec_pt = rec_pt.as<int>(); D.rec_id = rec_id.as<int>(); D.rec_r = rec_r.as<double>();
     D.data = data.as<double>(); D.datav = datav.as<double>(); D.dataw = dataw.as<double>();
 
+    d_desc = DevMem(&ctx, sizeof(PropDesc));
     if (s.mode == MODE_FWD && s.energy_every > 0 && s.nt / s.energy_every > 0)
         energy = DevMem(&ctx, (size_t)(s.nt / s.energy_every) * sizeof(double));
     if (s.T > 0 && s.wf) {
@@ -363,6 +364,16 @@ void Prop::reset(Context& ctx)
         MNAD_CK(cudaMemsetAsync(image.get(), 0, image.size(), st));
     }
     if (energy.get()) MNAD_CK(cudaMemsetAsync(energy.get(), 0, energy.size(), st));
+}
+
+void Prop::start(Context& ctx, int s_off)
+{
+    if (s_off & 1) throw Error(MNAD_E_STATE, "propagations start at even global steps");
+    desc.s_off = s_off;
+    upload(ctx, d_desc.get(), &desc, sizeof(PropDesc));
+    reset(ctx);
+    seed_sources<<<1, 32, 0, ctx.stream>>>(d_desc.as<PropDesc>(), 1);
+    MNAD_CK(cudaGetLastError());
 }
 
 double Prop::algorithmic_bytes() const
@@ -455,18 +466,12 @@ void Batch::finalize()
             upload(ctx_, g->tile_info.get(), info.data(), info.size() * sizeof(int4));
         }
     }
-    if (tc_.kind == MNAD_KERNEL_TMA)
-        d_counters_ = DevMem(&ctx_, std::max<size_t>(1, (size_t)nsteps_ * groups_.size()) * sizeof(int));
-    for (Prop* p : props_)
-        if (p->energy.get()) {
-            p->d_desc = DevMem(&ctx_, sizeof(PropDesc));
-            upload(ctx_, p->d_desc.get(), &p->desc, sizeof(PropDesc));
-        }
+    for (Prop* p : props_) upload(ctx_, p->d_desc.get(), &p->desc, sizeof(PropDesc));
     d_all_desc_ = DevMem(&ctx_, std::max<size_t>(1, all.size()) * sizeof(PropDesc));
     upload(ctx_, d_all_desc_.get(), all.data(), all.size() * sizeof(PropDesc));
 }
 
-void Batch::launch_step(int s)
+void Batch::launch_step(int s, int slot)
 {
     for (size_t gi = 0; gi < groups_.size(); ++gi) {
         auto& g = groups_[gi];
@@ -477,7 +482,7 @@ void Batch::launch_step(int s)
         a.tile_prop = g->tile_prop.as<int>();
         a.tmaps = g->tmaps.get();
         a.tile_info = g->tile_info.as<int4>();
-        a.tile_counter = d_counters_.as<int>() + (d_counters_.get() ? (size_t)s * groups_.size() + gi : 0);
+        a.tile_counter = d_counters_.as<int>() + (d_counters_.get() ? (size_t)slot * groups_.size() + gi : 0);
         a.ntiles = g->ntiles;
         a.ntz = g->props.empty() ? 0 : g->props[0]->desc.ntz;
         a.tiles_per_prop = g->props.empty() ? 0 : g->props[0]->desc.ntz * g->props[0]->desc.ntx;
@@ -494,7 +499,6 @@ void Batch::launch_step(int s)
 void Batch::start()
 {
     for (Prop* p : props_) p->reset(ctx_);
-    if (d_counters_.get()) MNAD_CK(cudaMemsetAsync(d_counters_.get(), 0, d_counters_.size(), ctx_.stream));
     if (!props_.empty())
         seed_sources<<<((int)props_.size() + 127) / 128, 128, 0, ctx_.stream>>>(d_all_desc_.as<PropDesc>(),
                                                                             (int)props_.size());
@@ -506,8 +510,8 @@ void Batch::encode_snapshots(int s)
     for (Prop* p : props_) {
         const PropSpec& sp = p->spec;
         if (sp.mode != MODE_FWD || !sp.wf || sp.wf->codec != MNAD_SNAP_F16 || sp.T <= 0) continue;
-        const int tt = s + 1;
-        if (tt > sp.nt || tt % sp.T != 0 || tt / sp.T > sp.wf->nsnap) continue;
+        const int tt = s - p->desc.s_off + 1;
+        if (tt < 1 || tt > sp.nt || tt % sp.T != 0 || tt / sp.T > sp.wf->nsnap) continue;
         const int k = tt / sp.T - 1;
         Wavefield& wf = *sp.wf;
         const size_t n = wf.nint;
@@ -522,12 +526,13 @@ void Batch::energy_after(int s)
 {
     for (Prop* p : props_) {
         const int K = p->spec.energy_every;
-        if (!p->energy.get() || (s + 1) % K != 0 || s + 1 > p->spec.nt) continue;
+        const int sl = s - p->desc.s_off;
+        if (!p->energy.get() || sl < 0 || (sl + 1) % K != 0 || sl + 1 > p->spec.nt) continue;
         const size_t n = p->nint();
         const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)ctx_.num_sms * 2);
         // after step s the new fields are time level (s + 1) & 1
         energy_reduce<<<std::max(blocks, 1), 256, 0, ctx_.stream>>>(p->d_desc.as<PropDesc>(), (s + 1) & 1,
-                                                                    p->energy.as<double>() + (s + 1) / K - 1);
+                                                                    p->energy.as<double>() + (sl + 1) / K - 1);
     }
 }
 
@@ -539,8 +544,14 @@ void Batch::advance(int s0, int s1)
         f16 |= p->spec.mode == MODE_FWD && p->spec.wf && p->spec.wf->codec == MNAD_SNAP_F16;
         en |= p->energy.get() != nullptr;
     }
+    if (tc_.kind == MNAD_KERNEL_TMA && s1 > s0) {
+        // one tile counter per step and group, zeroed before these launches
+        const size_t need = (size_t)(s1 - s0) * groups_.size() * sizeof(int);
+        if (d_counters_.size() < need) d_counters_ = DevMem(&ctx_, need);
+        MNAD_CK(cudaMemsetAsync(d_counters_.get(), 0, need, ctx_.stream));
+    }
     for (int s = s0; s < s1; ++s) {
-        launch_step(s);
+        launch_step(s, s - s0);
         if (f16) encode_snapshots(s);
         if (en) energy_after(s);
     }

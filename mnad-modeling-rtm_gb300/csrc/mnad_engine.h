@@ -108,6 +108,7 @@ struct Prop {
     DevMem energy, d_desc;             // energy history; this propagation's descriptor on the device
     void build(Context& ctx, const TileCfg& tc);
     void reset(Context& ctx);          // zero the state of a fresh run (stream-ordered)
+    void start(Context& ctx, int s_off);   // reset + seed the source; run from global step s_off (even)
     size_t nint() const { return (size_t)(spec.nz - 2 * spec.d) * (spec.nx - 2 * spec.d); }
     double point_updates() const { return (double)spec.nz * spec.nx * spec.nt; }
     double algorithmic_bytes() const;
@@ -133,12 +134,12 @@ public:
     void finalize();
     void run(bool use_graph);          // start() + every step, optionally as one CUDA graph (async)
     void start();                      // zero all state and seed the sources (async)
-    void advance(int s0, int s1);      // launch steps s0..s1-1 (async)
+    void advance(int s0, int s1);      // launch global steps s0..s1-1 (async)
     int steps() const { return nsteps_; }
     int tiles() const { return ntiles_; }
     const std::vector<Prop*>& props() const { return props_; }
 private:
-    void launch_step(int s);
+    void launch_step(int s, int slot);
     void encode_snapshots(int s);      // FP16 codec: encode the snapshots taken at step s
     void energy_after(int s);          // energy diagnostic after step s
     Context& ctx_;

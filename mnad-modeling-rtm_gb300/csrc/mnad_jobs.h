@@ -1,0 +1,48 @@
+// Argument checking, error capture and job set-up shared by the C ABI entry
+// points (mnad_capi.cu) and the serving loop (mnad_server.cu).  Internal.
+#pragma once
+#include <memory>
+#include <new>
+#include <string>
+
+#include "mnad_engine.h"
+
+namespace mnad {
+
+// Message of the last failed call on this thread (mnad_last_error).
+std::string& last_error();
+
+// Runs f, turning exceptions into status codes (the C ABI never throws).
+template <class F>
+int guard(F&& f)
+{
+    try {
+        f();
+        return MNAD_OK;
+    } catch (const Error& e) {
+        last_error() = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        last_error() = "host allocation failed";
+        return MNAD_E_OOM;
+    } catch (const std::exception& e) {
+        last_error() = e.what();
+        return MNAD_E_CUDA;
+    }
+}
+
+void need(bool ok, const std::string& msg);
+// 1-based grid index passed as a double (MATLAB) -> 0-based int.
+int index1(double x, int n, const char* what);
+void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, const double* v);
+void check_job(const mnad_job& j, int k);
+void fill_receivers(PropSpec& s, const double* xr, const double* zr, int nr);
+std::unique_ptr<Wavefield> new_wavefield(Context& c, int nz, int nx, int d, int nt, int T, int ncols, int nsnap,
+                                         int codec);
+// Snapshot interval of an RTM job (job.T or the reference formula on vs)
+// and the UU column count max(2 nf + 1, floor(nt/T)).
+void rtm_snapshot_plan(const mnad_job& j, int& T, int& ncols);
+// Propagation spec of a job: forward (true or background model) or adjoint.
+PropSpec job_spec(const mnad_job& j, int mode, const double* v, Wavefield* wf, int T, int pairing);
+
+}  // namespace mnad

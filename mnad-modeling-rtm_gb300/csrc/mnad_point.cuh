@@ -18,9 +18,12 @@ __device__ __forceinline__ void load_desc(PropDesc& dst, const PropDesc* src)
 
 // Current time index of a propagation at global step s (1-based tt), or 0
 // when it has no work at this step.
+// The local step is s - s_off; s_off is even, so the time level s & 1 is the
+// same for every propagation of a launch.
 __device__ __forceinline__ int step_tt(const PropDesc& P, int s)
 {
-    if (s >= P.nt) return 0;
+    s -= P.s_off;
+    if (s < 0 || s >= P.nt) return 0;
     return P.mode == MODE_FWD ? s + 1 : P.nt - s;
 }
 
