@@ -224,6 +224,52 @@ MNAD_API int mnad_plan_timing(const mnad_plan* plan, double* run_ms, double* ste
  * must share the grid.  Each output is Nint FP64 on the host, may be NULL. */
 MNAD_API int mnad_plan_stack(mnad_plan* plan, double* image_sum, double* illum_sum, double* img_rtm);
 
+/* ---- serving loop (continuous batching) -------------------------------- */
+/* A server owns a worker thread and a private context on one device.  Jobs
+ * (the mnad_job of mnad_run_jobs; inputs are copied at submission, outputs
+ * are written into the job's host pointers before the job completes) are
+ * admitted in arrival order while their device state fits the HBM budget,
+ * and every admitted propagation -- of any grid and record length -- advances
+ * chunk_steps time steps per tick of the worker, so jobs that arrive while
+ * others run join them at the next tick.  RTM jobs run the same three
+ * propagations as mnad_run_jobs (the background forward keeps its snapshots
+ * on the device until the adjoint has imaged them).  A job's outputs are
+ * bitwise those of the same job run alone. */
+typedef struct mnad_server mnad_server;
+typedef struct mnad_server_options {
+    size_t hbm_budget_bytes;  /* 0: 90% of the device's free memory */
+    int chunk_steps;          /* time steps per tick (rounded up to even; <= 0: 64) */
+    int max_active_jobs;      /* <= 0: limited by the budget only */
+    int snapshot_codec;       /* MNAD_SNAP_* of RTM snapshots */
+    int kernel;               /* MNAD_KERNEL_* */
+} mnad_server_options;
+
+enum { MNAD_JOB_QUEUED = 0, MNAD_JOB_RUNNING = 1, MNAD_JOB_DONE = 2, MNAD_JOB_FAILED = 3 };
+
+typedef struct mnad_server_stats {
+    int64_t submitted, completed, failed, queued;
+    double p50_ms, p99_ms, max_ms;  /* submission -> outputs on the host, completed jobs */
+    double point_updates;           /* grid-point updates of the completed jobs */
+    double busy_s;                  /* worker time spent in ticks */
+    double wall_s;                  /* since the first submission */
+    size_t bytes_in_use;            /* device memory held by the server now */
+} mnad_server_stats;
+
+MNAD_API int mnad_server_create(int device, const mnad_server_options* opt, mnad_server** out);
+/* Copies the job's inputs and queues it; *ticket identifies it.  Invalid
+ * jobs fail here with MNAD_E_ARG. */
+MNAD_API int mnad_server_submit(mnad_server* srv, const mnad_job* job, uint64_t* ticket);
+/* *state = MNAD_JOB_*. */
+MNAD_API int mnad_server_poll(mnad_server* srv, uint64_t ticket, int* state);
+/* Waits until the job completes (timeout_s < 0: no limit) and returns its
+ * status: MNAD_OK, the error it failed with, or MNAD_E_TIMEOUT when the
+ * wait ran out (the job keeps running).  A job larger than the whole budget
+ * fails with MNAD_E_BUDGET. */
+MNAD_API int mnad_server_wait(mnad_server* srv, uint64_t ticket, double timeout_s);
+MNAD_API int mnad_server_get_stats(mnad_server* srv, mnad_server_stats* stats);
+/* Finishes every submitted job, then stops the worker and frees the server. */
+MNAD_API int mnad_server_destroy(mnad_server* srv);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,7 +8,7 @@
 * :mod:`mnad.build` -- the nvcc build recipe of the library.
 """
 from ._lib import MnadError, lib  # noqa: F401
-from .api import Context, Plan, ShotJob  # noqa: F401
+from .api import Context, Plan, Server, ShotJob  # noqa: F401
 from .reference_api import Born_adj_MNAD, fwd_PDE_exact_MNAD  # noqa: F401
 
-__all__ = ["Context", "Plan", "ShotJob", "MnadError", "fwd_PDE_exact_MNAD", "Born_adj_MNAD", "lib"]
+__all__ = ["Context", "Plan", "Server", "ShotJob", "MnadError", "fwd_PDE_exact_MNAD", "Born_adj_MNAD", "lib"]

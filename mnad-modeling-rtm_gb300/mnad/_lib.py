@@ -18,6 +18,7 @@ SNAP_F32, SNAP_BF16, SNAP_F16 = 0, 1, 2
 PAIR_REFERENCE, PAIR_ALIGNED = 0, 1
 KERNEL_AUTO, KERNEL_DIRECT, KERNEL_TMA = 0, 1, 2
 JOB_MODEL, JOB_RTM = 0, 1
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 
 _CODE_NAMES = {E_ARG: "arg", E_OOM: "oom", E_CUDA: "cuda", E_TIMEOUT: "timeout", E_NOTFOUND: "notfound",
                E_NUMERIC: "numeric", E_BUDGET: "budget", E_STATE: "state"}
@@ -39,6 +40,18 @@ class Job(C.Structure):
                 ("v", _dp), ("vs", _dp), ("zs", C.c_double), ("xs", C.c_double),
                 ("nr", C.c_int), ("zr", _dp), ("xr", _dp), ("w", _dp), ("T", C.c_int),
                 ("data_out", _dp), ("image_out", _dp), ("illum_out", _dp)]
+
+
+class ServerOptions(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("chunk_steps", C.c_int), ("max_active_jobs", C.c_int),
+                ("snapshot_codec", C.c_int), ("kernel", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
+                ("point_updates", C.c_double), ("busy_s", C.c_double), ("wall_s", C.c_double),
+                ("bytes_in_use", C.c_size_t)]
 
 
 SIGNATURES = {
@@ -76,6 +89,12 @@ SIGNATURES = {
     "mnad_plan_work": ([_vp, _dp, _dp], C.c_int),
     "mnad_plan_timing": ([_vp, _dp, _dp, C.POINTER(C.c_int)], C.c_int),
     "mnad_plan_stack": ([_vp, _dp, _dp, _dp], C.c_int),
+    "mnad_server_create": ([C.c_int, C.POINTER(ServerOptions), C.POINTER(_vp)], C.c_int),
+    "mnad_server_submit": ([_vp, C.POINTER(Job), C.POINTER(C.c_uint64)], C.c_int),
+    "mnad_server_poll": ([_vp, C.c_uint64, C.POINTER(C.c_int)], C.c_int),
+    "mnad_server_wait": ([_vp, C.c_uint64, C.c_double], C.c_int),
+    "mnad_server_get_stats": ([_vp, C.POINTER(ServerStats)], C.c_int),
+    "mnad_server_destroy": ([_vp], C.c_int),
 }
 
 

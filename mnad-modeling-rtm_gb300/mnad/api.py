@@ -323,3 +323,68 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Continuous-batching server on one device (``mnad_server_*``).
+
+    ``submit`` copies a :class:`ShotJob`'s inputs and queues it; the worker
+    writes the outputs into the job's arrays, which this object keeps alive
+    until ``wait`` has seen the job finish.
+    """
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, chunk_steps: int = 64, max_active_jobs: int = 0,
+                 snapshot_codec: str = "f32", kernel: str = "auto"):
+        o = _lib.ServerOptions()
+        o.hbm_budget_bytes = int(hbm_budget_bytes)
+        o.chunk_steps = int(chunk_steps)
+        o.max_active_jobs = int(max_active_jobs)
+        o.snapshot_codec = _CODECS[snapshot_codec]
+        o.kernel = _KERNELS[kernel]
+        h = C.c_void_p()
+        check(lib().mnad_server_create(int(device), C.byref(o), C.byref(h)))
+        self._h = h
+        self._jobs = {}
+
+    def submit(self, job: ShotJob) -> int:
+        arr, _ = _job_array([job])
+        t = C.c_uint64()
+        check(lib().mnad_server_submit(self._h, arr, C.byref(t)))
+        self._jobs[t.value] = job
+        return t.value
+
+    def poll(self, ticket: int) -> str:
+        s = C.c_int()
+        check(lib().mnad_server_poll(self._h, int(ticket), C.byref(s)))
+        return ("queued", "running", "done", "failed")[s.value]
+
+    def wait(self, ticket: int, timeout_s: float = -1.0) -> ShotJob:
+        """Block until the job is done and return it (raises its error)."""
+        rc = lib().mnad_server_wait(self._h, int(ticket), float(timeout_s))
+        if rc != _lib.E_TIMEOUT:
+            job = self._jobs.pop(int(ticket), None)
+        check(rc)
+        return job
+
+    def stats(self) -> dict:
+        s = _lib.ServerStats()
+        check(lib().mnad_server_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in _lib.ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(lib().mnad_server_destroy(self._h))
+            self._h = None
+            self._jobs.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
