@@ -15,6 +15,9 @@ e2e      : same metric through the public C ABI (mnad_run_jobs) with host
            buffers, host<->device copies inside the timed region.
 plain    : the single-shot drop-in path (mnad_fwd_pde_exact x2 +
            mnad_born_adj per shot, serial), same metric.
+serving  : the served shot stream (Poisson arrivals of mixed modeling / RTM
+           jobs of four grid sizes and three record lengths) through the
+           continuous-batching server: throughput, p50/p99 job latency.
 --impl reference : the reference algorithm (literal FP64 sparse-operator
            restatement) on the host cores, shots in a process pool.
 """
@@ -51,6 +54,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, plain and CPU legs")
     ap.add_argument("--ref-steps", type=int, default=12, help="reference arm: time steps per worker sample")
     ap.add_argument("--kernel", default="auto", choices=["auto", "direct", "tma"])
+    ap.add_argument("--serve-jobs", type=int, default=512, help="served stream length (0: skip the leg)")
+    ap.add_argument("--serve-rate", type=float, default=None, help="arrivals per second (default: from the seed)")
     return ap.parse_args()
 
 
@@ -203,6 +208,71 @@ def plain_path(ctx, sv, nshots):
             "shots": nshots, "seconds": el}
 
 
+def serving_leg(device, njobs, rate=None, seed=0, kernel="auto"):
+    """Served shot stream through mnad.Server: a submitter thread replays the
+    Poisson schedule in real time, the main thread collects completions.
+    Throughput counts the grid-point updates of all jobs over the wall time
+    from the first arrival to the last completion."""
+    import threading
+    import numpy as np
+    import mnad
+    from mnad import workflow
+    sched, pools, rate = workflow.config4(seed=seed, njobs=njobs, rate=rate)
+    # warm-up server (module load, first allocations of the memory pool)
+    with mnad.Server(device, kernel=kernel) as w:
+        for sj in sched[:4]:
+            w.wait(w.submit(workflow.served_shot_job(workflow.ServedJob(0, sj.kind, (256, 256), 200, sj.fc, 0, 100),
+                                                     pools)), timeout_s=600)
+    srv = mnad.Server(device, kernel=kernel, chunk_steps=64)
+    tickets = [None] * len(sched)
+    ready = threading.Semaphore(0)
+    err = []
+
+    def submitter():
+        t0 = time.perf_counter()
+        try:
+            for k, sj in enumerate(sched):
+                job = workflow.served_shot_job(sj, pools)
+                delay = sj.arrival_s - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                tickets[k] = srv.submit(job)
+                ready.release()
+        except Exception as e:     # surfaced by the collector
+            err.append(e)
+            for _ in range(len(sched)):
+                ready.release()
+
+    th = threading.Thread(target=submitter)
+    t_start = time.perf_counter()
+    th.start()
+    bad = 0
+    kinds = {"model": 0, "rtm": 0}
+    for k in range(len(sched)):
+        ready.acquire()
+        if err:
+            break
+        job = srv.wait(tickets[k], timeout_s=3600)
+        kinds[job.kind] += 1
+        if not np.all(np.isfinite(job.data)) or (job.kind == "rtm" and not np.all(np.isfinite(job.image))):
+            bad += 1
+    th.join()
+    wall = time.perf_counter() - t_start
+    st = srv.stats()
+    srv.close()
+    if err:
+        raise err[0]
+    return {"workload": "served shot stream, config 4", "jobs": len(sched), "model_jobs": kinds["model"],
+            "rtm_jobs": kinds["rtm"], "arrival_rate_per_s": round(rate, 3),
+            "grids": [f"{g[0]}x{g[1]}" for g in workflow.SERVED_GRIDS], "seconds": list(workflow.SERVED_SECONDS),
+            "value": round(st["point_updates"] / wall / 1e9, 3), "unit": "Gpts/s",
+            "jobs_per_s": round(st["completed"] / wall, 3),
+            "rtm_jobs_per_hr": round(kinds["rtm"] / wall * 3600.0, 1),
+            "p50_ms": round(st["p50_ms"], 1), "p99_ms": round(st["p99_ms"], 1), "max_ms": round(st["max_ms"], 1),
+            "wall_s": round(wall, 2), "busy_s": round(st["busy_s"], 2), "failed": st["failed"],
+            "non_finite_outputs": bad, "snapshots": "f32", "chunk_steps": 64}
+
+
 def run_ours(args):
     import numpy as np
     rank, world, local = dist_setup(args.gpus)
@@ -270,6 +340,8 @@ def run_ours(args):
         if rank == 0:
             extras["cpu_baseline"] = cpu_baseline(sv)
     ctx.close()
+    if rank == 0 and args.serve_jobs > 0 and not args.no_extras:
+        extras["serving"] = serving_leg(local, args.serve_jobs, args.serve_rate, kernel=args.kernel)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Gpts/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 2),

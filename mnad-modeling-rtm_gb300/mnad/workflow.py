@@ -160,3 +160,79 @@ def shot_jobs(sv: Survey, kind: str = "rtm", shots=None, keep_data: bool = False
                            nt=sv.nt, d_pml=sv.d_pml, zs=sh.zs, xs=sh.xs, zr=sh.zr, xr=sh.xr, w=sv.w, T=sv.T,
                            keep_data=keep_data))
     return out
+
+
+# Served shot stream: grids (nz, nx) of the total (CPML-padded) model.
+SERVED_GRIDS = ((256, 256), (256, 512), (512, 1024), (1024, 2048))
+SERVED_SECONDS = (1.0, 2.0, 4.0)
+
+
+def layered_anomaly_model(nz: int, nx: int, h: float, rng) -> np.ndarray:
+    """Random layered model (3-6 layers, increasing with depth, 1500-4500 m/s)
+    with a Gaussian anomaly of +-(150-400) m/s, clipped to 1500-4500 m/s."""
+    nl = int(rng.integers(3, 7))
+    tops = np.sort(rng.uniform(0.1, 0.9, nl - 1)) * nz
+    vel = np.sort(rng.uniform(1500.0, 4500.0, nl))
+    z = np.arange(nz, dtype=np.float64)[:, None]
+    x = np.arange(nx, dtype=np.float64)[None, :]
+    layer = np.searchsorted(tops, z, side="right") * np.ones((1, nx), dtype=np.int64)
+    V = vel[layer]
+    cz, cx = rng.uniform(0.2, 0.8) * nz, rng.uniform(0.2, 0.8) * nx
+    sig = rng.uniform(100.0, 300.0) / h
+    amp = rng.uniform(150.0, 400.0) * rng.choice((-1.0, 1.0))
+    V = V + amp * np.exp(-((z - cz) ** 2 + (x - cx) ** 2) / (2 * sig ** 2))
+    return np.clip(V, 1500.0, 4500.0)
+
+
+@dataclass
+class ServedJob:
+    arrival_s: float
+    kind: str
+    grid: tuple
+    nt: int
+    fc: float
+    model: int        # index into the stream's model pool of that grid
+    xs: int           # 1-based padded source column
+
+
+def config4(seed: int = 0, njobs: int = 512, rate: Optional[float] = None, models_per_grid: int = 4,
+            d_pml: int = 20):
+    """Served shot stream: Poisson arrivals of ``njobs`` jobs, 70 % modeling
+    and 30 % RTM, grids drawn uniformly from SERVED_GRIDS at 10 m, record
+    lengths from SERVED_SECONDS at dt = 1 ms, Ricker 10-30 Hz, random
+    layered-plus-Gaussian-anomaly models in 1500-4500 m/s (a seeded pool of
+    ``models_per_grid`` per grid; migration models are their 9-point Gaussian
+    smoothing).  The arrival rate (jobs/s) is drawn from the seed in [10, 20]
+    unless given.  Returns (schedule, pools) where pools[grid] = [(v, vs)]."""
+    rng = np.random.default_rng(seed)
+    rate = float(rng.uniform(10.0, 20.0)) if rate is None else float(rate)
+    h = 10.0
+    pools = {}
+    for g in SERVED_GRIDS:
+        pools[g] = []
+        for _ in range(models_per_grid):
+            v = layered_anomaly_model(g[0], g[1], h, rng)
+            pools[g].append((v, gaussian_smooth(v, 9)))
+    t = 0.0
+    sched = []
+    for _ in range(njobs):
+        t += float(rng.exponential(1.0 / rate))
+        g = SERVED_GRIDS[int(rng.integers(len(SERVED_GRIDS)))]
+        kind = "model" if rng.random() < 0.7 else "rtm"
+        nt = int(round(SERVED_SECONDS[int(rng.integers(len(SERVED_SECONDS)))] / 1e-3))
+        sched.append(ServedJob(t, kind, g, nt, float(rng.uniform(10.0, 30.0)), int(rng.integers(models_per_grid)),
+                               int(rng.integers(d_pml + 2, g[1] - d_pml))))
+    return sched, pools, rate
+
+
+def served_shot_job(sj: ServedJob, pools, d_pml: int = 20):
+    """ShotJob of one stream entry: source one row below the CPML at column
+    ``xs``, receivers on every column of the first physical row + 1."""
+    from .api import ShotJob
+    v, vs = pools[sj.grid][sj.model]
+    nz, nx = sj.grid
+    xr = np.arange(d_pml + 1, nx - d_pml + 1, dtype=np.float64)
+    zr = np.full(xr.size, float(d_pml + 2))
+    return ShotJob(kind=sj.kind, v=v, vs=vs if sj.kind == "rtm" else None, dx=10.0, dz=10.0, dt=1e-3, nt=sj.nt,
+                   d_pml=d_pml, zs=float(d_pml + 2), xs=float(sj.xs), zr=zr, xr=xr, w=ricker(sj.fc, 1e-3, sj.nt),
+                   keep_data=True)
