@@ -536,6 +536,13 @@ void Batch::energy_after(int s)
     }
 }
 
+size_t Batch::reserve_counters(int nsteps)
+{
+    const size_t need = (size_t)std::max(nsteps, 1) * std::max<size_t>(groups_.size(), 1) * sizeof(int);
+    if (d_counters_.size() < need) d_counters_ = DevMem(&ctx_, need);
+    return need;
+}
+
 void Batch::advance(int s0, int s1)
 {
     if (ntiles_ == 0) return;
@@ -546,8 +553,7 @@ void Batch::advance(int s0, int s1)
     }
     if (tc_.kind == MNAD_KERNEL_TMA && s1 > s0) {
         // one tile counter per step and group, zeroed before these launches
-        const size_t need = (size_t)(s1 - s0) * groups_.size() * sizeof(int);
-        if (d_counters_.size() < need) d_counters_ = DevMem(&ctx_, need);
+        const size_t need = reserve_counters(s1 - s0);
         MNAD_CK(cudaMemsetAsync(d_counters_.get(), 0, need, ctx_.stream));
     }
     for (int s = s0; s < s1; ++s) {
@@ -571,6 +577,9 @@ void Batch::run(bool use_graph)
         return;
     }
     if (!graph_) {
+        // allocate outside the capture: a graph that allocates memory cannot
+        // be relaunched while that memory is held
+        if (tc_.kind == MNAD_KERNEL_TMA) reserve_counters(nsteps_);
         cudaGraph_t g = nullptr;
         MNAD_CK(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal));
         body();

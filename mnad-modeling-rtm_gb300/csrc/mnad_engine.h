@@ -140,6 +140,7 @@ public:
     const std::vector<Prop*>& props() const { return props_; }
 private:
     void launch_step(int s, int slot);
+    size_t reserve_counters(int nsteps);   // tile counters for nsteps steps (bytes used)
     void encode_snapshots(int s);      // FP16 codec: encode the snapshots taken at step s
     void energy_after(int s);          // energy diagnostic after step s
     Context& ctx_;
