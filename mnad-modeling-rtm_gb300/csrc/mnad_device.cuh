@@ -88,6 +88,9 @@ struct __align__(16) PropDesc {
     const int* rec_id;       // receiver column rr of each entry
     const double* rec_r;     // r at the receiver (adjoint injection scale)
     const int* tile_rec;     // [ntz*ntx + 1]
+    const int* col_rec;      // [ntz*ntx*TX + 1]: entries of local column c of tile t
+                             // are col_rec[t*TX + c] .. col_rec[t*TX + c+1] (TX: the
+                             // tile width of the kernel the propagation was built for)
     double* data;            // [nr][nt] (column-major nt x nr): fwd out / adj in
     double* datav;           // optional fwd outputs
     double* dataw;
@@ -116,8 +119,16 @@ struct Coefs {
 };
 
 // Arguments of one step launch: the propagations of one (dx, dz) group.
+// The same coefficients as (c, c) pairs for packed FP32x2 arithmetic over two
+// z-points; the entries that the update applies with a negative sign (K_UV_X1
+// of alpha and beta, K_UV_D of beta) are stored negated.
+struct Coefs2 {
+    float2 alpha[NCOEF], beta[NCOEF];
+};
+
 struct StepArgs {
     Coefs coef;
+    Coefs2 coef2;          // TMA kernel
     const PropDesc* props;
     const int* tile_prop;
     const void* tmaps;     // CUtensorMap[nprops][TMAPS_PER_PROP] (TMA kernel)

@@ -285,26 +285,33 @@ void Prop::build(Context& ctx, const TileCfg& tc)
         D.src_amp = src_amp.as<float>();
     }
 
-    // Receivers bucketed by tile (counting sort).
+    // Receivers bucketed by tile and, within a tile, by column (stable
+    // counting sort): the entries of tile t are tile_rec[t] .. tile_rec[t+1],
+    // those of its local column c are col_rec[t*tx + c] .. col_rec[t*tx + c+1].
     const int nr = (int)s.zr.size();
     const int ntiles = D.ntz * D.ntx;
-    std::vector<int> cnt(ntiles + 1, 0), pt(nr), id(nr);
+    const int nb = ntiles * tc.tx;
+    std::vector<int> cnt(nb + 1, 0), pt(nr), id(nr);
     std::vector<double> rr(nr);
-    for (int k = 0; k < nr; ++k) cnt[1 + (s.zr[k] / tc.tz) + (s.xr[k] / tc.tx) * D.ntz]++;
-    for (int t = 0; t < ntiles; ++t) cnt[t + 1] += cnt[t];
+    auto bucket = [&](int k) { return ((s.zr[k] / tc.tz) + (s.xr[k] / tc.tx) * D.ntz) * tc.tx + s.xr[k] % tc.tx; };
+    for (int k = 0; k < nr; ++k) cnt[1 + bucket(k)]++;
+    for (int b = 0; b < nb; ++b) cnt[b + 1] += cnt[b];
     std::vector<int> fill(cnt.begin(), cnt.end() - 1);
     for (int k = 0; k < nr; ++k) {
-        const int t = (s.zr[k] / tc.tz) + (s.xr[k] / tc.tx) * D.ntz;
-        const int e = fill[t]++;
+        const int e = fill[bucket(k)]++;
         pt[e] = off(s.zr[k], s.xr[k]);
         id[e] = k;
         rr[e] = r_of(s.v[(size_t)s.zr[k] + (size_t)s.xr[k] * nz], s.dt, s.mode);
     }
     D.nr = nr;
-    tile_rec_host = cnt;
+    tile_rec_host.assign(ntiles + 1, 0);
+    for (int t = 0; t <= ntiles; ++t) tile_rec_host[t] = cnt[(size_t)t * tc.tx];
     tile_rec = DevMem(&ctx, (ntiles + 1) * sizeof(int));
-    upload(ctx, tile_rec.get(), cnt.data(), (ntiles + 1) * sizeof(int));
+    upload(ctx, tile_rec.get(), tile_rec_host.data(), (ntiles + 1) * sizeof(int));
     D.tile_rec = tile_rec.as<int>();
+    col_rec = DevMem(&ctx, (size_t)(nb + 1) * sizeof(int));
+    upload(ctx, col_rec.get(), cnt.data(), (size_t)(nb + 1) * sizeof(int));
+    D.col_rec = col_rec.as<int>();
     if (nr > 0) {
         rec_pt = DevMem(&ctx, nr * sizeof(int));
         rec_id = DevMem(&ctx, nr * sizeof(int));
@@ -449,7 +456,12 @@ void Batch::finalize()
                     const int tl = tz + tx * D.ntz;
                     const int rb = p->tile_rec_host[tl], re = p->tile_rec_host[tl + 1];
                     if (j0 >= (1 << 16) || i0 >= (1 << 15)) throw Error(MNAD_E_ARG, "grid too large for the TMA tiling");
-                    info.push_back(make_int4(rb, re, (interior ? 0 : TILE_STRIP) | (re > rb ? TILE_RECEIVERS : 0),
+                    // the source, or a z/x neighbour whose CPML term sees it
+                    const int zs = p->spec.zs, xs = p->spec.xs;
+                    const bool src = D.src >= 0 && zs >= j0 - 1 && zs <= j0 + TMA_TZ && xs >= i0 - 1 &&
+                                     xs <= i0 + TMA_TX;
+                    info.push_back(make_int4(rb, re, (interior ? 0 : TILE_STRIP) | (re > rb ? TILE_RECEIVERS : 0) |
+                                                         (src ? TILE_SOURCE : 0),
                                              j0 | (i0 << 16)));
                 }
         }
@@ -478,6 +490,11 @@ void Batch::launch_step(int s, int slot)
         if (g->ntiles == 0) continue;
         StepArgs a;
         a.coef = g->coefs;
+        for (int k = 0; k < NCOEF; ++k) {
+            const float sa = k == K_UV_X1 ? -1.0f : 1.0f, sb = (k == K_UV_X1 || k == K_UV_D) ? -1.0f : 1.0f;
+            a.coef2.alpha[k] = make_float2(sa * g->coefs.alpha[k], sa * g->coefs.alpha[k]);
+            a.coef2.beta[k] = make_float2(sb * g->coefs.beta[k], sb * g->coefs.beta[k]);
+        }
         a.props = g->desc.as<PropDesc>();
         a.tile_prop = g->tile_prop.as<int>();
         a.tmaps = g->tmaps.get();

@@ -104,7 +104,7 @@ struct Prop {
     Coefs coefs{};                     // stencil polynomials of (dx, dz)
     size_t S = 0;                      // floats per field in storage
     std::vector<int> tile_rec_host;    // receiver bucket offsets per tile
-    DevMem fields, r, mx, mz, src_amp, rec_pt, rec_id, rec_r, tile_rec, data, datav, dataw, image;
+    DevMem fields, r, mx, mz, src_amp, rec_pt, rec_id, rec_r, tile_rec, col_rec, data, datav, dataw, image;
     DevMem energy, d_desc;             // energy history; this propagation's descriptor on the device
     void build(Context& ctx, const TileCfg& tc);
     void reset(Context& ctx);          // zero the state of a fresh run (stream-ordered)

@@ -24,6 +24,7 @@ constexpr int TMAP_HALO = 0, TMAP_POINT = 6, TMAP_R = 12, TMAPS_PER_PROP = 13;
 // tile_info.z flags
 constexpr int TILE_STRIP = 1;         // intersects a CPML strip or the grid edge
 constexpr int TILE_RECEIVERS = 2;     // has receivers
+constexpr int TILE_SOURCE = 4;        // the source point or one of its z/x neighbours
 
 __global__ void step_direct(const __grid_constant__ StepArgs A);
 __global__ void step_tma(const __grid_constant__ StepArgs A);

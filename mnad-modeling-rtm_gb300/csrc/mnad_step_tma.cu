@@ -182,117 +182,176 @@ struct Window {
         wz[0] = st.halo[2][c][r0 - 2];
         wz[1] = st.halo[2][c][r0 + TMA_PZ + 1];
     }
-    __device__ __forceinline__ void hood(int k, Hood& h) const
-    {
-        h.u00 = u[1][k + 1]; h.uzm = u[1][k]; h.uzp = u[1][k + 2]; h.uxm = u[0][k + 1]; h.uxp = u[2][k + 1];
-        h.umm = u[0][k]; h.upm = u[0][k + 2]; h.ump = u[2][k]; h.upp = u[2][k + 2];
-        h.v00 = v[1][k + 1]; h.vzm = v[1][k]; h.vzp = v[1][k + 2]; h.vxm = v[0][k + 1]; h.vxp = v[2][k + 1];
-        h.vmm = v[0][k]; h.vpm = v[0][k + 2]; h.vmp = v[2][k]; h.vpp = v[2][k + 2];
-        h.vxm2 = v2m[k]; h.vxp2 = v2p[k];
-        h.w00 = w[1][k + 1]; h.wzm = w[1][k]; h.wzp = w[1][k + 2]; h.wxm = w[0][k + 1]; h.wxp = w[2][k + 1];
-        h.wmm = w[0][k]; h.wpm = w[0][k + 2]; h.wmp = w[2][k]; h.wpp = w[2][k + 2];
-        h.wzm2 = k == 0 ? wz[0] : w[1][k - 1];
-        h.wzp2 = k == TMA_PZ - 1 ? wz[1] : w[1][k + 3];
-    }
 };
 
-// The stencil sums su, sv, sw (see mnad_update) of the TMA_PZ points of a
-// thread, with the combinations of the side columns shared between rows:
-// per row r, S = F(c-1) + F(c+1) and D = F(c-1) - F(c+1), so that e.g. the
-// diagonal sum of point k is S[k] + S[k+2] and the odd diagonal of
-// Avu_gen.m is D[k] + D[k+2].
-__device__ __forceinline__ void mnad_update_window(const Coefs& K, const Window& win, const float* rr, float* su,
-                                                   float* sv, float* sw)
+// Packed FP32x2 arithmetic (one instruction for two z-points).  Each lane is
+// the IEEE operation of the scalar form, so results do not depend on the
+// packing.
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b)
 {
-    constexpr int R = Window::R;
-    const float* a = K.alpha;
-    const float* b = K.beta;
-    float SU[R], DU[R], SV[R], DV[R], SW[R], DW[R];
+    unsigned long long x = *reinterpret_cast<unsigned long long*>(&a);
+    unsigned long long y = *reinterpret_cast<unsigned long long*>(&b), z;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(z) : "l"(x), "l"(y));
+    return *reinterpret_cast<float2*>(&z);
+}
+__device__ __forceinline__ float2 pr(float a, float b) { return make_float2(a, b); }
+
+// The stencil sums su, sv, sw (see mnad_update) of the 4 points of a thread,
+// as two z-pairs (points 0,1 and 2,3).  Side columns enter through their
+// row sums S = F(c-1) + F(c+1) and differences D = F(c-1) - F(c+1), shared
+// between rows: e.g. the diagonal sum of point k is S[k] + S[k+2] and the odd
+// diagonal of Avu_gen.m is D[k] + D[k+2].  Per point the operations, their
+// order and their rounding are those of mnad_update.
+__device__ __forceinline__ void mnad_update_pairs(const Coefs2& K, const Window& win, const float* rr, float2* su,
+                                                  float2* sv, float2* sw)
+{
+    static_assert(TMA_PZ == 4, "two z-pairs per thread");
+    const float2* a = K.alpha;
+    const float2* b = K.beta;
+    const float* U = win.u[1];
+    const float* V = win.v[1];
+    const float* W = win.w[1];
+    // row sums / differences of the side columns: rows 1..4 as pairs, rows 0 and 5 alone
+    float2 SUp[2], DUp[2], SVp[2], DVp[2], SWp[2], DWp[2];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        SU[r] = win.u[0][r] + win.u[2][r]; DU[r] = win.u[0][r] - win.u[2][r];
-        SV[r] = win.v[0][r] + win.v[2][r]; DV[r] = win.v[0][r] - win.v[2][r];
-        SW[r] = win.w[0][r] + win.w[2][r]; DW[r] = win.w[0][r] - win.w[2][r];
+    for (int m = 0; m < 2; ++m) {
+        const int r = 1 + 2 * m;
+        SUp[m] = padd(pr(win.u[0][r], win.u[0][r + 1]), pr(win.u[2][r], win.u[2][r + 1]));
+        DUp[m] = psub(pr(win.u[0][r], win.u[0][r + 1]), pr(win.u[2][r], win.u[2][r + 1]));
+        SVp[m] = padd(pr(win.v[0][r], win.v[0][r + 1]), pr(win.v[2][r], win.v[2][r + 1]));
+        DVp[m] = psub(pr(win.v[0][r], win.v[0][r + 1]), pr(win.v[2][r], win.v[2][r + 1]));
+        SWp[m] = padd(pr(win.w[0][r], win.w[0][r + 1]), pr(win.w[2][r], win.w[2][r + 1]));
+        DWp[m] = psub(pr(win.w[0][r], win.w[0][r + 1]), pr(win.w[2][r], win.w[2][r + 1]));
+    }
+    float SU[6], DU[6], SV[6], DV[6], SW[6], DW[6];
+    SU[0] = win.u[0][0] + win.u[2][0]; DU[0] = win.u[0][0] - win.u[2][0];
+    SV[0] = win.v[0][0] + win.v[2][0]; DV[0] = win.v[0][0] - win.v[2][0];
+    SW[0] = win.w[0][0] + win.w[2][0]; DW[0] = win.w[0][0] - win.w[2][0];
+    SU[5] = win.u[0][5] + win.u[2][5]; DU[5] = win.u[0][5] - win.u[2][5];
+    SV[5] = win.v[0][5] + win.v[2][5]; DV[5] = win.v[0][5] - win.v[2][5];
+    SW[5] = win.w[0][5] + win.w[2][5]; DW[5] = win.w[0][5] - win.w[2][5];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        SU[1 + 2 * m] = SUp[m].x; SU[2 + 2 * m] = SUp[m].y; DU[1 + 2 * m] = DUp[m].x; DU[2 + 2 * m] = DUp[m].y;
+        SV[1 + 2 * m] = SVp[m].x; SV[2 + 2 * m] = SVp[m].y; DV[1 + 2 * m] = DVp[m].x; DV[2 + 2 * m] = DVp[m].y;
+        SW[1 + 2 * m] = SWp[m].x; SW[2 + 2 * m] = SWp[m].y; DW[1 + 2 * m] = DWp[m].x; DW[2 + 2 * m] = DWp[m].y;
     }
 #pragma unroll
-    for (int k = 0; k < TMA_PZ; ++k) {
-        const float r = rr[k], q = r * r;
-        const float u0 = win.u[1][k + 1], v0 = win.v[1][k + 1], w0 = win.w[1][k + 1];
-        const float u2 = u0 + u0, v2 = v0 + v0, w2 = w0 + w0;
-        const float uzs = win.u[1][k] + win.u[1][k + 2], vzs = win.v[1][k] + win.v[1][k + 2];
-        const float wzs = win.w[1][k] + win.w[1][k + 2];
+    for (int m = 0; m < 2; ++m) {
+        const int k = 2 * m;              // points k, k+1 (window rows k+1, k+2)
+        const float2 r = pr(rr[k], rr[k + 1]);
+        const float2 q = pmul(r, r);
+        const float2 u0 = pr(U[k + 1], U[k + 2]), v0 = pr(V[k + 1], V[k + 2]), w0 = pr(W[k + 1], W[k + 2]);
+        const float2 u2 = padd(u0, u0), v2 = padd(v0, v0), w2 = padd(w0, w0);
+        const float2 uzs = pr(U[k] + U[k + 2], U[k + 1] + U[k + 3]);
+        const float2 vzs = pr(V[k] + V[k + 2], V[k + 1] + V[k + 3]);
+        const float2 wzs = pr(W[k] + W[k + 2], W[k + 1] + W[k + 3]);
         // U combinations (Auu, Avu, Awu)
-        const float dUz = uzs - u2, dUx = SU[k + 1] - u2, dUd = (SU[k] + SU[k + 2]) - (u2 + u2);
-        const float uLx = DU[k + 1], uLz = win.u[1][k] - win.u[1][k + 2];
-        const float uDx = DU[k] + DU[k + 2], uDz = SU[k] - SU[k + 2];
+        const float2 dUz = psub(uzs, u2), dUx = psub(SUp[m], u2);
+        const float2 dUd = psub(pr(SU[k] + SU[k + 2], SU[k + 1] + SU[k + 3]), padd(u2, u2));
+        const float2 uLx = DUp[m], uLz = pr(U[k] - U[k + 2], U[k + 1] - U[k + 3]);
+        const float2 uDx = pr(DU[k] + DU[k + 2], DU[k + 1] + DU[k + 3]);
+        const float2 uDz = pr(SU[k] - SU[k + 2], SU[k + 1] - SU[k + 3]);
         // V combinations (Avv, Auv, Awv); vX1 and vDx enter with negative sign
-        const float dVz = vzs - v2, dVx = SV[k + 1] - v2, dVd = (SV[k] + SV[k + 2]) - (v2 + v2);
-        const float nvX1 = DV[k + 1], nvDx = DV[k] + DV[k + 2];
-        const float vX2 = win.v2m[k] - win.v2p[k], vXZ = DV[k] - DV[k + 2];
+        const float2 dVz = psub(vzs, v2), dVx = psub(SVp[m], v2);
+        const float2 dVd = psub(pr(SV[k] + SV[k + 2], SV[k + 1] + SV[k + 3]), padd(v2, v2));
+        const float2 nvX1 = DVp[m], nvDx = pr(DV[k] + DV[k + 2], DV[k + 1] + DV[k + 3]);
+        const float2 vX2 = psub(pr(win.v2m[k], win.v2m[k + 1]), pr(win.v2p[k], win.v2p[k + 1]));
+        const float2 vXZ = pr(DV[k] - DV[k + 2], DV[k + 1] - DV[k + 3]);
         // W combinations (Aww, Auw, Avw)
-        const float wzm2 = k == 0 ? win.wz[0] : win.w[1][k - 1];
-        const float wzp2 = k == TMA_PZ - 1 ? win.wz[1] : win.w[1][k + 3];
-        const float dWz = wzs - w2, dWx = SW[k + 1] - w2, dWd = (SW[k] + SW[k + 2]) - (w2 + w2);
-        const float wZ1 = win.w[1][k + 2] - win.w[1][k], wDz = SW[k + 2] - SW[k];
-        const float wZ2 = wzm2 - wzp2, wXZ = DW[k] - DW[k + 2];
+        const float2 wzm2 = m == 0 ? pr(win.wz[0], W[0]) : pr(W[1], W[2]);
+        const float2 wzp2 = m == 0 ? pr(W[3], W[4]) : pr(W[5], win.wz[1]);
+        const float2 dWz = psub(wzs, w2), dWx = psub(SWp[m], w2);
+        const float2 dWd = psub(pr(SW[k] + SW[k + 2], SW[k + 1] + SW[k + 3]), padd(w2, w2));
+        const float2 wZ1 = pr(W[k + 2] - W[k], W[k + 3] - W[k + 1]);
+        const float2 wDz = pr(SW[k + 2] - SW[k], SW[k + 3] - SW[k + 1]);
+        const float2 wZ2 = psub(wzm2, wzp2), wXZ = pr(DW[k] - DW[k + 2], DW[k + 1] - DW[k + 3]);
         // nU row
-        float ra = a[K_UU_Z] * dUz;
-        ra = fmaf(a[K_UU_X], dUx, ra);
-        ra = fmaf(-a[K_UV_X1], nvX1, ra);
-        ra = fmaf(a[K_UV_X2], vX2, ra);
-        ra = fmaf(a[K_UW_Z1], wZ1, ra);
-        ra = fmaf(a[K_UW_Z2], wZ2, ra);
-        float qa = b[K_UU_Z] * dUz;
-        qa = fmaf(b[K_UU_X], dUx, qa);
-        qa = fmaf(b[K_UU_D], dUd, qa);
-        qa = fmaf(-b[K_UV_X1], nvX1, qa);
-        qa = fmaf(-b[K_UV_D], nvDx, qa);
-        qa = fmaf(b[K_UV_X2], vX2, qa);
-        qa = fmaf(b[K_UW_Z1], wZ1, qa);
-        qa = fmaf(b[K_UW_D], wDz, qa);
-        qa = fmaf(b[K_UW_Z2], wZ2, qa);
-        su[k] = fmaf(q, qa, r * ra);
+        float2 ra = pmul(a[K_UU_Z], dUz);
+        ra = pfma(a[K_UU_X], dUx, ra);
+        ra = pfma(a[K_UV_X1], nvX1, ra);       // negated pair
+        ra = pfma(a[K_UV_X2], vX2, ra);
+        ra = pfma(a[K_UW_Z1], wZ1, ra);
+        ra = pfma(a[K_UW_Z2], wZ2, ra);
+        float2 qa = pmul(b[K_UU_Z], dUz);
+        qa = pfma(b[K_UU_X], dUx, qa);
+        qa = pfma(b[K_UU_D], dUd, qa);
+        qa = pfma(b[K_UV_X1], nvX1, qa);       // negated pair
+        qa = pfma(b[K_UV_D], nvDx, qa);        // negated pair
+        qa = pfma(b[K_UV_X2], vX2, qa);
+        qa = pfma(b[K_UW_Z1], wZ1, qa);
+        qa = pfma(b[K_UW_D], wDz, qa);
+        qa = pfma(b[K_UW_Z2], wZ2, qa);
+        su[m] = pfma(q, qa, pmul(r, ra));
         // nV row
-        float rb = a[K_VV_Z] * dVz;
-        rb = fmaf(a[K_VV_X], dVx, rb);
-        rb = fmaf(a[K_VV_R], v0, rb);
-        rb = fmaf(a[K_VU_X1], uLx, rb);
-        rb = fmaf(a[K_VU_D], uDx, rb);
-        rb = fmaf(a[K_VW], wXZ, rb);
-        float qb = b[K_VV_Z] * dVz;
-        qb = fmaf(b[K_VV_X], dVx, qb);
-        qb = fmaf(b[K_VV_D], dVd, qb);
-        qb = fmaf(b[K_VV_R], v0, qb);
-        qb = fmaf(b[K_VU_X1], uLx, qb);
-        qb = fmaf(b[K_VU_D], uDx, qb);
-        qb = fmaf(b[K_VW], wXZ, qb);
-        sv[k] = fmaf(q, qb, r * rb);
+        float2 rb = pmul(a[K_VV_Z], dVz);
+        rb = pfma(a[K_VV_X], dVx, rb);
+        rb = pfma(a[K_VV_R], v0, rb);
+        rb = pfma(a[K_VU_X1], uLx, rb);
+        rb = pfma(a[K_VU_D], uDx, rb);
+        rb = pfma(a[K_VW], wXZ, rb);
+        float2 qb = pmul(b[K_VV_Z], dVz);
+        qb = pfma(b[K_VV_X], dVx, qb);
+        qb = pfma(b[K_VV_D], dVd, qb);
+        qb = pfma(b[K_VV_R], v0, qb);
+        qb = pfma(b[K_VU_X1], uLx, qb);
+        qb = pfma(b[K_VU_D], uDx, qb);
+        qb = pfma(b[K_VW], wXZ, qb);
+        sv[m] = pfma(q, qb, pmul(r, rb));
         // nW row
-        float rc = a[K_WW_Z] * dWz;
-        rc = fmaf(a[K_WW_X], dWx, rc);
-        rc = fmaf(a[K_WW_R], w0, rc);
-        rc = fmaf(a[K_WU_Z1], uLz, rc);
-        rc = fmaf(a[K_WU_D], uDz, rc);
-        rc = fmaf(a[K_WV], vXZ, rc);
-        float qc = b[K_WW_Z] * dWz;
-        qc = fmaf(b[K_WW_X], dWx, qc);
-        qc = fmaf(b[K_WW_D], dWd, qc);
-        qc = fmaf(b[K_WW_R], w0, qc);
-        qc = fmaf(b[K_WU_Z1], uLz, qc);
-        qc = fmaf(b[K_WU_D], uDz, qc);
-        qc = fmaf(b[K_WV], vXZ, qc);
-        sw[k] = fmaf(q, qc, r * rc);
+        float2 rc = pmul(a[K_WW_Z], dWz);
+        rc = pfma(a[K_WW_X], dWx, rc);
+        rc = pfma(a[K_WW_R], w0, rc);
+        rc = pfma(a[K_WU_Z1], uLz, rc);
+        rc = pfma(a[K_WU_D], uDz, rc);
+        rc = pfma(a[K_WV], vXZ, rc);
+        float2 qc = pmul(b[K_WW_Z], dWz);
+        qc = pfma(b[K_WW_X], dWx, qc);
+        qc = pfma(b[K_WW_D], dWd, qc);
+        qc = pfma(b[K_WW_R], w0, qc);
+        qc = pfma(b[K_WU_Z1], uLz, qc);
+        qc = pfma(b[K_WU_D], uDz, qc);
+        qc = pfma(b[K_WV], vXZ, qc);
+        sw[m] = pfma(q, qc, pmul(r, rc));
     }
 }
 
-// Receiver injection of the adjoint at storage offset p (entries rbeg..rend).
-__device__ __forceinline__ float injection(const PropDesc& P, int tt, int rbeg, int rend, int p)
+// Forward receiver sampling (fwd_PDE_exact_MNAD.m:119-123) of the entries
+// rbeg..rend of a tile, read from the stage: its halo boxes hold the current
+// U, V, W of every point of the tile.
+__device__ __forceinline__ void record_tile(const PropDesc& P, const Stage& st, int tt, int rbeg, int rend, int j0,
+                                            int i0)
 {
-    float inj = 0.0f;
-    for (int e = rbeg; e < rend; ++e)
-        if (__ldg(P.rec_pt + e) == p)
-            inj += (float)(__ldg(P.rec_r + e) * __ldg(P.data + (size_t)__ldg(P.rec_id + e) * P.nt + tt));
-    return inj;
+    for (int e = rbeg + (int)threadIdx.x; e < rend; e += TMA_THREADS) {
+        const int pt = __ldg(P.rec_pt + e);
+        const int ic = pt / P.ld, jr = pt - ic * P.ld;          // storage column / row
+        const int cx = ic - HX - i0 + 2, rz = jr - HZ - j0 + 4; // position in the halo box
+        const size_t o = (size_t)__ldg(P.rec_id + e) * P.nt + (tt - 1);
+        const float u = st.halo[0][cx][rz];
+        if (!isfinite(u)) atomicOr(P.status, ST_NONFINITE);
+        P.data[o] = u;
+        if (P.datav) P.datav[o] = st.halo[1][cx][rz];
+        if (P.dataw) P.dataw[o] = st.halo[2][cx][rz];
+    }
+}
+
+// Adjoint receiver injection r*data(tt+1) of the TMA_PZ points p.. of local
+// column c of tile tl: only the entries of that column are scanned, in entry
+// order, so receivers at one point add up in the order of the whole list.
+__device__ __forceinline__ void injection(const PropDesc& P, int tt, int tl, int c, int p, float* inj)
+{
+    const int cb = __ldg(P.col_rec + tl * TMA_TX + c), ce = __ldg(P.col_rec + tl * TMA_TX + c + 1);
+    for (int e = cb; e < ce; ++e) {
+        const int k = __ldg(P.rec_pt + e) - p;
+        if (k < 0 || k >= TMA_PZ) continue;
+        const float x = (float)(__ldg(P.rec_r + e) * __ldg(P.data + (size_t)__ldg(P.rec_id + e) * P.nt + tt));
+#pragma unroll
+        for (int q = 0; q < TMA_PZ; ++q)
+            if (q == k) inj[q] += x;
+    }
 }
 
 }  // namespace
@@ -317,14 +376,14 @@ __device__ __forceinline__ void cpml_c(float K, float vel, float X, float dt, fl
 // U, V, W into cu, cv, cw.  U is taken before this step's source injection
 // (fwd_PDE_exact_MNAD.m:95-111): the stored U already holds it.
 __device__ __forceinline__ void cpml_vec(const PropDesc& P, const Stage& st, int c, int r0, int tt, int j, int i,
-                                         int p, const float* r, float* cu, float* cv, float* cw)
+                                         int p, bool has_src, const float* r, float* cu, float* cv, float* cw)
 {
     constexpr int Q = TMA_PZ;
     const int d = P.d, nz = P.nz, nx = P.nx, ld = P.ld;
     float vel[Q];
 #pragma unroll
     for (int k = 0; k < Q; ++k) vel[k] = r[k] * rsqrtf(r[k]) * P.inv_dt;
-    const float srcamp = (P.mode == MODE_FWD && P.src >= 0) ? P.src_amp[tt - 1] : 0.0f;
+    const float srcamp = (has_src && P.mode == MODE_FWD && P.src >= 0) ? P.src_amp[tt - 1] : 0.0f;
     const int src = P.src;
     if (d <= 0) return;                 // no CPML strips (and no memory-variable storage)
     // x direction: the whole column lies in the strip
@@ -461,7 +520,6 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
         }
     const int tzt = tid % TMA_TZY, txt = tid / TMA_TZY;
     const int c = txt + 2, r0 = tzt * TMA_PZ + 4;
-    const Coefs& K = A.coef;
     bool producing = true;
 
     for (int n = 0;; ++n) {
@@ -481,21 +539,54 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
         const int j0 = info.w & 0xffff, i0 = info.w >> 16;
         const int tl = j0 / TMA_TZ + (i0 / TMA_TX) * P.ntz;
         const int nz = P.nz, nx = P.nx, d = P.d, ld = P.ld, nt = P.nt, mode = P.mode;
-        if (tt != 0 && (info.z & TILE_RECEIVERS) && mode == MODE_FWD)
-            record_receivers(P, tt, tl, P.fld[cur][0], P.fld[cur][1], P.fld[cur][2]);
+        if (tt != 0 && (info.z & TILE_RECEIVERS) && mode == MODE_FWD) record_tile(P, st, tt, info.x, info.y, j0, i0);
         const int j = j0 + tzt * TMA_PZ;
         const int i = i0 + txt;
-        if (tt != 0 && j < nz && i < nx) {
+        // tt / T and tt % T without an integer division: (tt + 0.5) / T is
+        // never within 0.5/T of an integer, far beyond float rounding.
+        const int tq = (int)(((float)tt + 0.5f) * P.invT);
+        const bool snap_step = P.T > 0 && tt - tq * P.T == 0;
+        // A plain tile (image region only, no source, no receivers, no
+        // snapshot or imaging at this step) is stencil arithmetic and stores.
+        const bool plain = !(info.z & (TILE_STRIP | TILE_RECEIVERS | TILE_SOURCE)) && !snap_step;
+        if (tt != 0 && plain) {
+            constexpr int Q = TMA_PZ;
+            float rr[Q];
+            ldv(&st.pts[3][txt][tzt * Q], rr);
+            const int p = (i + HX) * ld + (j + HZ);
+            float2 su[2], sv[2], sw[2];
+            {
+                Window win;
+                win.load(st, c, r0);
+                mnad_update_pairs(A.coef2, win, rr, su, sv, sw);
+            }
+            const float4 pu = *reinterpret_cast<const float4*>(&st.pts[0][txt][tzt * Q]);
+            const float4 pv = *reinterpret_cast<const float4*>(&st.pts[1][txt][tzt * Q]);
+            const float4 pw = *reinterpret_cast<const float4*>(&st.pts[2][txt][tzt * Q]);
+            const float4 uc = *reinterpret_cast<const float4*>(&st.halo[0][c][r0]);
+            const float4 vc = *reinterpret_cast<const float4*>(&st.halo[1][c][r0]);
+            const float4 wc = *reinterpret_cast<const float4*>(&st.halo[2][c][r0]);
+            // nF = F + ((F - pF) + sF)
+            const float2 u01 = pr(uc.x, uc.y), u23 = pr(uc.z, uc.w);
+            const float2 v01 = pr(vc.x, vc.y), v23 = pr(vc.z, vc.w);
+            const float2 w01 = pr(wc.x, wc.y), w23 = pr(wc.z, wc.w);
+            const float2 nu01 = padd(u01, padd(psub(u01, pr(pu.x, pu.y)), su[0]));
+            const float2 nu23 = padd(u23, padd(psub(u23, pr(pu.z, pu.w)), su[1]));
+            const float2 nv01 = padd(v01, padd(psub(v01, pr(pv.x, pv.y)), sv[0]));
+            const float2 nv23 = padd(v23, padd(psub(v23, pr(pv.z, pv.w)), sv[1]));
+            const float2 nw01 = padd(w01, padd(psub(w01, pr(pw.x, pw.y)), sw[0]));
+            const float2 nw23 = padd(w23, padd(psub(w23, pr(pw.z, pw.w)), sw[1]));
+            *reinterpret_cast<float4*>(P.fld[cur ^ 1][0] + p) = make_float4(nu01.x, nu01.y, nu23.x, nu23.y);
+            *reinterpret_cast<float4*>(P.fld[cur ^ 1][1] + p) = make_float4(nv01.x, nv01.y, nv23.x, nv23.y);
+            *reinterpret_cast<float4*>(P.fld[cur ^ 1][2] + p) = make_float4(nw01.x, nw01.y, nw23.x, nw23.y);
+        } else if (tt != 0 && j < nz && i < nx) {
             constexpr int Q = TMA_PZ;
             float rr[Q];
             ldv(&st.pts[3][txt][tzt * Q], rr);
             const int p = (i + HX) * ld + (j + HZ);
             const int rbeg = info.x, rend = info.y;
             const bool adj_inj = mode == MODE_ADJ && tt < nt && rbeg < rend;
-            // tt / T and tt % T without an integer division: (tt + 0.5) / T is
-            // never within 0.5/T of an integer, far beyond float rounding.
-            const int tq = (int)(((float)tt + 0.5f) * P.invT);
-            const bool snap_step = P.T > 0 && tt - tq * P.T == 0;
+            const bool has_src = (info.z & TILE_SOURCE) != 0;
             const int niz = nz - 2 * d;
             const size_t nint = (size_t)niz * (nx - 2 * d);
             const long long q0 = (long long)(j - d) + (long long)(i - d) * niz;
@@ -506,20 +597,25 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                 if (col < 1 || col > P.nsnap) col = 0;
             }
             const int src = P.src;
-            const float src_next = (mode == MODE_FWD && src >= p && src < p + Q && tt < nt) ? P.src_amp[tt] : 0.0f;
+            const float src_next = (has_src && mode == MODE_FWD && src >= p && src < p + Q && tt < nt)
+                                       ? P.src_amp[tt] : 0.0f;
             // lean: every point of the group inside the image region (no CPML, no edge)
             const bool lean = i >= d && i < nx - d && j >= d && j + Q - 1 < nz - d;
             float su[Q], sv[Q], sw[Q];
             {
                 Window win;            // dies here: later phases re-read the stage
                 win.load(st, c, r0);
-                mnad_update_window(K, win, rr, su, sv, sw);
+                float2 s2u[2], s2v[2], s2w[2];
+                mnad_update_pairs(A.coef2, win, rr, s2u, s2v, s2w);
+                su[0] = s2u[0].x; su[1] = s2u[0].y; su[2] = s2u[1].x; su[3] = s2u[1].y;
+                sv[0] = s2v[0].x; sv[1] = s2v[0].y; sv[2] = s2v[1].x; sv[3] = s2v[1].y;
+                sw[0] = s2w[0].x; sw[1] = s2w[0].y; sw[2] = s2w[1].x; sw[3] = s2w[1].y;
             }
             if (!lean) {
                 float cu[Q], cv[Q], cw[Q];
 #pragma unroll
                 for (int k = 0; k < Q; ++k) cu[k] = cv[k] = cw[k] = 0.0f;
-                cpml_vec(P, st, c, r0, tt, j, i, p, rr, cu, cv, cw);
+                cpml_vec(P, st, c, r0, tt, j, i, p, has_src, rr, cu, cv, cw);
 #pragma unroll
                 for (int k = 0; k < Q; ++k) {
                     su[k] = fmaf(-rr[k], cu[k], su[k]);
@@ -537,17 +633,20 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
             float ou[Q], ov[Q], ow[Q];
 #pragma unroll
             for (int k = 0; k < Q; ++k) {
-                const int jk = j + k;
-                const bool inner = lean || (jk >= d && jk < nz - d && i >= d && i < nx - d);
                 const float u0 = uc[k], v0 = vc[k], w0 = wc[k];
-                float xu = u0 + ((u0 - pu[k]) + su[k]);
-                float xv = v0 + ((v0 - pv[k]) + sv[k]);
-                float xw = w0 + ((w0 - pw[k]) + sw[k]);
-                if (mode == MODE_FWD) {
-                    if (snap_step && inner) {
+                ou[k] = u0 + ((u0 - pu[k]) + su[k]);
+                ov[k] = v0 + ((v0 - pv[k]) + sv[k]);
+                ow[k] = w0 + ((w0 - pw[k]) + sw[k]);
+            }
+            if (mode == MODE_FWD) {
+                if (snap_step) {
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) {
+                        const int jk = j + k;
+                        if (!(jk >= d && jk < nz - d && i >= d && i < nx - d)) continue;
                         // fwd_PDE_exact_MNAD.m:128-141; nU - 2U + pU = su
                         float d2u = su[k];
-                        if (tt == 1) d2u = fmaf(2.0f, u0, su[k] - pu[k]);
+                        if (tt == 1) d2u = fmaf(2.0f, uc[k], su[k] - pu[k]);
                         else if (tt == 2) d2u = su[k] - pu[k];
                         d2u *= P.inv_dt2;
                         const size_t q = (size_t)(q0 + k);
@@ -556,20 +655,37 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                         else static_cast<float*>(P.snap)[o] = d2u;
                         P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
                     }
-                    if (p + k == src) xu += src_next;
-                } else {
-                    if (adj_inj) xu -= injection(P, tt, rbeg, rend, p + k);
-                    if (col && inner) {
+                }
+                if (src_next != 0.0f) {
+#pragma unroll
+                    for (int k = 0; k < Q; ++k)
+                        if (p + k == src) ou[k] += src_next;
+                }
+            } else {
+                if (adj_inj) {
+                    float inj[Q];
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) inj[k] = 0.0f;
+                    injection(P, tt, tl, txt, p, inj);
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) ou[k] -= inj[k];
+                }
+                if (col) {
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) {
+                        const int jk = j + k;
+                        if (!(jk >= d && jk < nz - d && i >= d && i < nx - d)) continue;
                         const size_t q = (size_t)(q0 + k);
                         const float sc = P.codec == CODEC_F16 ? P.snap_scale[col - 1] : 1.0f;
                         const float us = snap_decode(P.snap, P.codec, (size_t)(col - 1) * nint + q, sc);
-                        P.image[q] = fma((double)us, (double)xu, P.image[q]);
+                        P.image[q] = fma((double)us, (double)ou[k], P.image[q]);
                     }
                 }
-                if (jk >= nz) xu = xv = xw = 0.0f;   // rows past nz are the zero halo
-                ou[k] = xu;
-                ov[k] = xv;
-                ow[k] = xw;
+            }
+            if (j + Q > nz) {
+#pragma unroll
+                for (int k = 0; k < Q; ++k)
+                    if (j + k >= nz) ou[k] = ov[k] = ow[k] = 0.0f;   // rows past nz are the zero halo
             }
             stv(P.fld[cur ^ 1][0] + p, ou);
             stv(P.fld[cur ^ 1][1] + p, ov);
