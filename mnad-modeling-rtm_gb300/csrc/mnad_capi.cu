@@ -4,6 +4,8 @@
 #include "mnad_kernels.h"
 
 #include <algorithm>
+#include <map>
+#include <tuple>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -396,6 +398,9 @@ struct mnad_plan {
     std::vector<std::unique_ptr<Prop>> props;            // owns every propagation
     std::vector<Prop*> fwd_true, fwd_bg, adj;            // per job (nullptr where not used)
     std::vector<std::unique_ptr<Wavefield>> wfs;
+    // r of each distinct (host model, grid, dt, mode): shots that pass the same
+    // model array share one upload and one device copy
+    std::map<std::tuple<const double*, int, int, double, int>, DevMem> rcache;
     std::unique_ptr<Batch> phase1, phase3;
     cudaEvent_t ev[4] = {};
     double pts = 0, bytes = 0;
@@ -450,6 +455,11 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
             }
         }
         for (auto& p : P->props) {
+            const PropSpec& sp = p->spec;
+            const auto key = std::make_tuple(sp.v, sp.nz, sp.nx, sp.dt, sp.mode);
+            auto it = P->rcache.find(key);
+            if (it == P->rcache.end()) it = P->rcache.emplace(key, make_r(c, sp.v, sp.nz, sp.nx, sp.dt, sp.mode)).first;
+            p->r_ext = it->second.as<float>();
             p->build(c, tc);
             (p->spec.mode == MODE_FWD ? P->phase1 : P->phase3)->add(p.get());
             P->pts += p->point_updates();

@@ -225,6 +225,21 @@ double r_of(double v, double dt, int mode)
 }
 
 // ---------------------------------------------------------------------------
+DevMem make_r(Context& ctx, const double* v, int nz, int nx, double dt, int mode)
+{
+    const int ld = (int)round_up((size_t)nz + HZ + HZB, 32);
+    const size_t S = (size_t)ld * (nx + 2 * HX);
+    DevMem r(&ctx, S * sizeof(float));
+    MNAD_CK(cudaMemsetAsync(r.get(), 0, r.size(), ctx.stream));
+    const size_t N = (size_t)nz * nx;
+    DevMem vt(&ctx, N * sizeof(double));
+    upload(ctx, vt.get(), v, N * sizeof(double));
+    const int blocks = (int)std::min<size_t>((N + 255) / 256, (size_t)ctx.num_sms * 8);
+    build_r<<<blocks, 256, 0, ctx.stream>>>(vt.as<double>(), nz, nx, dt, mode == MODE_ADJ, r.as<float>(), ld);
+    MNAD_CK(cudaGetLastError());
+    return r;
+}
+
 void Prop::build(Context& ctx, const TileCfg& tc)
 {
     const PropSpec& s = spec;
@@ -238,19 +253,10 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     cudaStream_t st = ctx.stream;
 
     fields = DevMem(&ctx, 6 * S * sizeof(float));
-    r = DevMem(&ctx, S * sizeof(float));
-    MNAD_CK(cudaMemsetAsync(r.get(), 0, r.size(), st));
+    if (!r_ext) r = make_r(ctx, s.v, nz, nx, s.dt, s.mode);
     if (d > 0) {
         mx = DevMem(&ctx, (size_t)2 * 9 * d * ld * sizeof(float));
         mz = DevMem(&ctx, (size_t)2 * 9 * nx * dpz * sizeof(float));
-    }
-    const size_t N = (size_t)nz * nx;
-    {
-        DevMem vt(&ctx, N * sizeof(double));
-        upload(ctx, vt.get(), s.v, N * sizeof(double));
-        const int blocks = (int)std::min<size_t>((N + 255) / 256, (size_t)ctx.num_sms * 8);
-        build_r<<<blocks, 256, 0, st>>>(vt.as<double>(), nz, nx, s.dt, s.mode == MODE_ADJ, r.as<float>(), ld);
-        MNAD_CK(cudaGetLastError());
     }
 
     PropDesc& D = desc;
@@ -260,7 +266,7 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     D.ntx = (nx + tc.tx - 1) / tc.tx;
     for (int t = 0; t < 2; ++t)
         for (int f = 0; f < 3; ++f) D.fld[t][f] = fields.as<float>() + (size_t)(t * 3 + f) * S;
-    D.r = r.as<float>();
+    D.r = r_ext ? r_ext : r.as<float>();
     D.mx = mx.as<float>();
     D.mz = mz.as<float>();
     const double R = 1e-4;   // fwd_PDE_exact_MNAD.m:88

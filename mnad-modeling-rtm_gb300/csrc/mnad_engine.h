@@ -106,6 +106,7 @@ struct Prop {
     std::vector<int> tile_rec_host;    // receiver bucket offsets per tile
     DevMem fields, r, mx, mz, src_amp, rec_pt, rec_id, rec_r, tile_rec, col_rec, data, datav, dataw, image;
     DevMem energy, d_desc;             // energy history; this propagation's descriptor on the device
+    const float* r_ext = nullptr;      // set before build(): r shared with other propagations
     void build(Context& ctx, const TileCfg& tc);
     void reset(Context& ctx);          // zero the state of a fresh run (stream-ordered)
     void start(Context& ctx, int s_off);   // reset + seed the source; run from global step s_off (even)
@@ -152,6 +153,10 @@ private:
     int ntiles_ = 0, nsteps_ = 0;
     cudaGraphExec_t graph_ = nullptr;
 };
+
+// r = v^2 dt^2 (forward) or (v dt)^2 (adjoint) of a host model, in padded
+// storage on the device.
+DevMem make_r(Context& ctx, const double* v, int nz, int nx, double dt, int mode);
 
 // Stencil coefficient polynomials of one grid spacing (centre entries as in
 // the Coef enum) and r = v^2 dt^2 as the forward / adjoint compute it.

@@ -39,7 +39,8 @@ void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, 
          "dx, dz, dt must be positive and finite");
     const size_t n = (size_t)nz * nx;
     for (size_t k = 0; k < n; ++k)
-        need(std::isfinite(v[k]) && v[k] > 0, "velocity must be positive and finite (entry " + std::to_string(k) + ")");
+        if (!(std::isfinite(v[k]) && v[k] > 0))   // the message is built only on failure
+            need(false, "velocity must be positive and finite (entry " + std::to_string(k) + ")");
 }
 
 std::unique_ptr<Wavefield> new_wavefield(Context& c, int nz, int nx, int d, int nt, int T, int ncols,

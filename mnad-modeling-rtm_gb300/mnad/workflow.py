@@ -154,10 +154,15 @@ def config3(seed: int = 0, nshots: int = 64, nt: int = 4000, codec: str = "bf16"
 def shot_jobs(sv: Survey, kind: str = "rtm", shots=None, keep_data: bool = False):
     """mnad.api.ShotJob list for a survey (RTM: true + migration model)."""
     from .api import ShotJob
+    # one column-major copy of each model shared by every job: the library
+    # uploads a model array once per plan however many shots use it
+    v = np.asfortranarray(sv.v, dtype=np.float64)
+    vs = np.asfortranarray(sv.vs, dtype=np.float64) if (kind == "rtm" and sv.vs is not None) else None
+    w = sv.w
     out = []
     for sh in (sv.shots if shots is None else shots):
-        out.append(ShotJob(kind=kind, v=sv.v, vs=sv.vs if kind == "rtm" else None, dx=sv.dx, dz=sv.dz, dt=sv.dt,
-                           nt=sv.nt, d_pml=sv.d_pml, zs=sh.zs, xs=sh.xs, zr=sh.zr, xr=sh.xr, w=sv.w, T=sv.T,
+        out.append(ShotJob(kind=kind, v=v, vs=vs, dx=sv.dx, dz=sv.dz, dt=sv.dt,
+                           nt=sv.nt, d_pml=sv.d_pml, zs=sh.zs, xs=sh.xs, zr=sh.zr, xr=sh.xr, w=w, T=sv.T,
                            keep_data=keep_data))
     return out
 
