@@ -77,6 +77,17 @@ typedef struct mnad_options {
     int kernel;           /* MNAD_KERNEL_*; default AUTO */
     int energy_every;     /* > 0: FP64 energy diagnostic of each forward every
                              that many steps (read with mnad_context_energy) */
+    int checkpoint_every; /* > 0: RTM jobs of a plan keep no snapshot history:
+                             the background forward saves its state every C
+                             steps (C = this value rounded up to an even
+                             multiple of T), and the adjoint runs in segments,
+                             each recomputing its C steps of source snapshots
+                             from a checkpoint into an FP32 buffer of C/T
+                             columns.  Default 0 (all snapshots kept). */
+    int checkpoint_codec; /* MNAD_SNAP_F32 (exact recompute: images identical
+                             to the stored-snapshot FP32 run) or MNAD_SNAP_F16
+                             (states stored in FP16 with one power-of-two scale
+                             per array); default MNAD_SNAP_F32 */
 } mnad_options;
 
 typedef struct mnad_context mnad_context;

@@ -4,6 +4,7 @@
 #include "mnad_kernels.h"
 
 #include <algorithm>
+#include <climits>
 #include <map>
 #include <tuple>
 #include <cmath>
@@ -51,6 +52,9 @@ MNAD_API int mnad_context_set_options(mnad_context* ctx, const mnad_options* o)
         need(o->pairing == MNAD_PAIR_REFERENCE || o->pairing == MNAD_PAIR_ALIGNED, "bad pairing");
         need(o->kernel >= MNAD_KERNEL_AUTO && o->kernel <= MNAD_KERNEL_TMA, "bad kernel");
         need(o->energy_every >= 0, "energy_every must be >= 0");
+        need(o->checkpoint_every >= 0, "checkpoint_every must be >= 0");
+        need(o->checkpoint_codec == MNAD_SNAP_F32 || o->checkpoint_codec == MNAD_SNAP_F16,
+             "checkpoint_codec must be MNAD_SNAP_F32 or MNAD_SNAP_F16");
         ctx->opt = *o;
     });
 }
@@ -402,6 +406,12 @@ struct mnad_plan {
     // model array share one upload and one device copy
     std::map<std::tuple<const double*, int, int, double, int>, DevMem> rcache;
     std::unique_ptr<Batch> phase1, phase3;
+    // checkpointed RTM (options.checkpoint_every > 0): per job the segment
+    // length C = m*T, the segment count G and the pairing offset delta
+    // (imaging column = tt/T + delta); `recomp` holds the background forwards
+    bool ckpt = false;
+    std::vector<int> ck_C, ck_m, ck_G, ck_delta;
+    std::unique_ptr<Batch> recomp;
     cudaEvent_t ev[4] = {};
     double pts = 0, bytes = 0;
     float run_ms = 0, step_ms = 0;
@@ -420,6 +430,86 @@ static Prop* add_prop(mnad_plan& P, const mnad_job& j, int mode, const double* v
     p->spec = job_spec(j, mode, v, wf, T, P.ctx->opt.pairing);
     P.props.push_back(std::move(p));
     return P.props.back().get();
+}
+
+// Adjoints of a checkpointed plan, segment by segment from the last: restore
+// every background forward from its checkpoint, recompute the segment's C
+// steps with snapshots into the C/T-column buffer, then run the adjoint steps
+// that image with exactly those snapshots.  Each propagation advances only in
+// its own window of global steps (s_begin, s_end), with s_off chosen so its
+// local step continues where it stands and its time level keeps the parity of
+// the global step.  Returns the number of step launches.
+static int run_segments(mnad_plan& P)
+{
+    Context& c = *P.ctx;
+    const size_t nj = P.jobs.size();
+    P.phase3->start();                              // zero adjoint states and images
+    int Gmax = 0;
+    for (size_t k = 0; k < nj; ++k)
+        if (P.adj[k]) Gmax = std::max(Gmax, P.ck_G[k]);
+    auto off = [](Prop* p) { p->desc.s_begin = p->desc.s_end = INT_MIN; };
+    for (size_t k = 0; k < nj; ++k)
+        if (P.fwd_bg[k]) P.fwd_bg[k]->ckpt.saving = false;   // the recomputation saves nothing
+    int R = 0, launches = 0;
+    for (int r = 0; r < Gmax; ++r) {
+        int L = 0;
+        for (size_t k = 0; k < nj; ++k) {
+            Prop* b = P.fwd_bg[k];
+            if (!b) continue;
+            const int g = P.ck_G[k] - 1 - r;
+            if (g < 0) { off(b); continue; }
+            b->restore_state(c, g);
+            const int a0 = g * P.ck_C[k], len = std::min(P.ck_C[k], P.jobs[k].nt - a0);
+            b->desc.s_off = R - a0;
+            b->desc.s_begin = R;
+            b->desc.s_end = R + len;
+            b->desc.snap_flags = SNAP_WRITE;
+            b->desc.snap_col0 = g * P.ck_m[k];
+            L = std::max(L, len);
+        }
+        P.recomp->refresh_descs();
+        P.recomp->advance(R, R + L);
+        launches += L;
+        R += L + (L & 1);
+        L = 0;
+        for (size_t k = 0; k < nj; ++k) {
+            Prop* a = P.adj[k];
+            if (!a) continue;
+            const int g = P.ck_G[k] - 1 - r;
+            if (g < 0) { off(a); continue; }
+            const int nt = P.jobs[k].nt, C = P.ck_C[k], Td = a->spec.T * P.ck_delta[k];
+            const int hi = g == P.ck_G[k] - 1 ? nt : (g + 1) * C - Td;
+            const int lo = std::max(0, g * C - Td);
+            const int sa = nt - hi, len = hi - lo;      // adjoint local steps sa .. sa + len - 1
+            const int Rj = R + (sa & 1);
+            a->desc.s_off = Rj - sa;
+            a->desc.s_begin = Rj;
+            a->desc.s_end = Rj + len;
+            a->desc.snap_col0 = g * P.ck_m[k];
+            L = std::max(L, (sa & 1) + len);
+        }
+        P.phase3->refresh_descs();
+        P.phase3->advance(R, R + L);
+        launches += L;
+        R += L + (L & 1);
+    }
+    // back to the whole-run descriptors for the next run
+    for (size_t k = 0; k < nj; ++k)
+        for (Prop* p : {P.fwd_bg[k], P.adj[k]}) {
+            if (!p) continue;
+            p->desc.s_off = 0;
+            p->desc.s_begin = INT_MIN;
+            p->desc.s_end = INT_MAX;
+            p->desc.snap_col0 = 0;
+            if (p->spec.mode == MODE_FWD) {
+                p->desc.snap_flags = SNAP_ILLUM;
+                p->ckpt.saving = true;
+            }
+        }
+    P.recomp->refresh_descs();
+    P.phase3->refresh_descs();
+    MNAD_CK(cudaGetLastError());
+    return launches;
 }
 
 extern "C" {
@@ -442,13 +532,34 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
         P->fwd_true.assign(njobs, nullptr);
         P->fwd_bg.assign(njobs, nullptr);
         P->adj.assign(njobs, nullptr);
+        P->ckpt = c.opt.checkpoint_every > 0;
+        P->ck_C.assign(njobs, 0);
+        P->ck_m.assign(njobs, 0);
+        P->ck_G.assign(njobs, 0);
+        P->ck_delta.assign(njobs, 0);
+        if (P->ckpt) P->recomp = std::make_unique<Batch>(c, tc);
         for (int k = 0; k < njobs; ++k) {
             const mnad_job& j = jobs[k];
             P->fwd_true[k] = add_prop(*P, j, MODE_FWD, j.v, nullptr, 0);
             if (j.kind == MNAD_JOB_RTM) {
                 int T, ncols;
                 rtm_snapshot_plan(j, T, ncols);
-                P->wfs.push_back(new_wavefield(c, j.nz, j.nx, j.d_pml, j.nt, T, ncols, j.nt / T, c.opt.snapshot_codec));
+                const int k_snap = j.nt / T;
+                if (P->ckpt) {
+                    // segments of C = m*T steps (C even, so a restored state keeps
+                    // its time-level parity); m > delta, so each adjoint chunk
+                    // images with the snapshots of one segment only
+                    const int delta = c.opt.pairing == MNAD_PAIR_REFERENCE ? ncols - k_snap : 0;
+                    int m = std::max((c.opt.checkpoint_every + T - 1) / T, delta + 1);
+                    if ((m * T) & 1) ++m;
+                    P->ck_C[k] = m * T;
+                    P->ck_m[k] = m;
+                    P->ck_G[k] = (j.nt + m * T - 1) / (m * T);
+                    P->ck_delta[k] = delta;
+                    P->wfs.push_back(new_wavefield(c, j.nz, j.nx, j.d_pml, j.nt, T, ncols, k_snap, MNAD_SNAP_F32, m));
+                } else {
+                    P->wfs.push_back(new_wavefield(c, j.nz, j.nx, j.d_pml, j.nt, T, ncols, k_snap, c.opt.snapshot_codec));
+                }
                 Wavefield* wf = P->wfs.back().get();
                 P->fwd_bg[k] = add_prop(*P, j, MODE_FWD, j.vs, wf, T);
                 P->adj[k] = add_prop(*P, j, MODE_ADJ, j.vs, wf, T);
@@ -465,6 +576,18 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
             P->pts += p->point_updates();
             P->bytes += p->algorithmic_bytes();
         }
+        if (P->ckpt)
+            for (int k = 0; k < njobs; ++k) {
+                Prop* b = P->fwd_bg[k];
+                if (!b) continue;
+                b->desc.snap_flags = SNAP_ILLUM;       // the full forward only accumulates illumination
+                b->setup_checkpoints(c, P->ck_C[k], P->ck_G[k], c.opt.checkpoint_codec);
+                b->ckpt.saving = true;
+                P->recomp->add(b);
+                P->pts += b->point_updates();           // the recomputation is work done too
+                P->bytes += b->algorithmic_bytes();
+            }
+        if (P->ckpt) P->recomp->finalize();
         P->phase1->finalize();
         P->phase3->finalize();
         for (auto& e : P->ev) MNAD_CK(cudaEventCreate(&e));
@@ -492,7 +615,9 @@ MNAD_API int mnad_plan_run(mnad_plan* P)
             MNAD_CK(cudaGetLastError());
         }
         MNAD_CK(cudaEventRecord(P->ev[2], c.stream));
-        P->phase3->run(g);
+        int seg_launches = 0;
+        if (P->ckpt) seg_launches = run_segments(*P);
+        else P->phase3->run(g);
         MNAD_CK(cudaEventRecord(P->ev[3], c.stream));
         MNAD_CK(cudaEventSynchronize(P->ev[3]));
         float a = 0, b = 0, t = 0;
@@ -501,7 +626,7 @@ MNAD_API int mnad_plan_run(mnad_plan* P)
         MNAD_CK(cudaEventElapsedTime(&b, P->ev[2], P->ev[3]));
         P->run_ms = t;
         P->step_ms = a + b;
-        P->launches = P->phase1->steps() + P->phase3->steps();
+        P->launches = P->phase1->steps() + (P->ckpt ? seg_launches : P->phase3->steps());
     });
 }
 

@@ -26,6 +26,7 @@ constexpr int HX = 2;   // zero columns on each side (V needs x +- 2)
 
 enum Mode { MODE_FWD = 0, MODE_ADJ = 1 };
 enum Codec { CODEC_F32 = 0, CODEC_BF16 = 1, CODEC_F16 = 2 };
+enum SnapFlags { SNAP_WRITE = 1, SNAP_ILLUM = 2 };
 enum Pairing { PAIR_REFERENCE = 0, PAIR_ALIGNED = 1 };
 
 // Status bits written by kernels (never traps).
@@ -70,6 +71,7 @@ struct __align__(16) PropDesc {
     int zb0;           // first storage row of the bottom z strip: (nz - d) rounded down to 4
     int tile_base;     // first global tile of this propagation
     int s_off;         // global step at which this propagation started (even)
+    int s_begin, s_end;  // global steps [s_begin, s_end) in which it may advance
     int ntz, ntx;      // tiles along z / x
     float* fld[2][3];  // [time level][U,V,W], storage origin (halo included)
     const float* r;    // v^2 dt^2, same storage
@@ -106,6 +108,10 @@ struct __align__(16) PropDesc {
     int snap_stage;          // forward with the FP16 codec: every snapshot is
                              // written in FP32 to one staging slot, then encoded
     const float* snap_scale; // per-snapshot scale (FP16 codec), may be null
+    int snap_col0;           // snapshot column (0-based) held in the first slot of `snap`
+    int snap_cols;           // slots of `snap`: a forward writes, an adjoint reads only
+                             // columns snap_col0 .. snap_col0 + snap_cols - 1
+    int snap_flags;          // forward: SNAP_WRITE | SNAP_ILLUM (checkpointed RTM runs them apart)
     double* illum;           // [nint] sum of d2u^2 (forward)
     double* image;           // [nint] sum of US.*UR (adjoint)
     float inv_dt2;

@@ -6,6 +6,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -62,6 +63,8 @@ Context::Context(int dev, size_t budget_bytes) : device(dev), budget(budget_byte
     opt.use_graphs = 1;
     opt.kernel = MNAD_KERNEL_AUTO;
     opt.energy_every = 0;
+    opt.checkpoint_every = 0;
+    opt.checkpoint_codec = MNAD_SNAP_F32;
 }
 
 Context::~Context()
@@ -261,6 +264,8 @@ void Prop::build(Context& ctx, const TileCfg& tc)
 
     PropDesc& D = desc;
     std::memset(&D, 0, sizeof(D));
+    D.s_begin = INT_MIN;
+    D.s_end = INT_MAX;
     D.mode = s.mode; D.nt = s.nt; D.nz = nz; D.nx = nx; D.ld = ld; D.d = d; D.dpz = dpz; D.zb0 = zb0;
     D.ntz = (nz + tc.tz - 1) / tc.tz;
     D.ntx = (nx + tc.tx - 1) / tc.tx;
@@ -347,10 +352,14 @@ void Prop::build(Context& ctx, const TileCfg& tc)
         D.pairing = s.pairing;
         D.snap = wf.snap.get();
         D.snap_scale = wf.scale.as<float>();
+        D.snap_col0 = 0;
+        D.snap_cols = wf.held;
+        D.snap_flags = SNAP_WRITE | SNAP_ILLUM;
         if (s.mode == MODE_FWD && wf.codec == MNAD_SNAP_F16) {
             D.snap = wf.stage.get();        // FP32 staging slot, encoded after each snapshot step
             D.codec = CODEC_F32;
             D.snap_stage = 1;
+            D.snap_cols = 1;
         }
         if (s.mode == MODE_FWD) {
             D.illum = wf.illum.as<double>();
@@ -386,6 +395,116 @@ void Prop::start(Context& ctx, int s_off)
     upload(ctx, d_desc.get(), &desc, sizeof(PropDesc));
     reset(ctx);
     seed_sources<<<1, 32, 0, ctx.stream>>>(d_desc.as<PropDesc>(), 1);
+    MNAD_CK(cudaGetLastError());
+}
+
+void Prop::setup_checkpoints(Context& ctx, int C, int G, int codec)
+{
+    Checkpoints& k = ckpt;
+    k.C = C;
+    k.G = G;
+    k.codec = codec;
+    const size_t nf = fields.size() / sizeof(float), nmx = mx.size() / sizeof(float), nmz = mz.size() / sizeof(float);
+    k.slot = nf + nmx + nmz;
+    k.blocks.clear();
+    for (int b = 0; b < 6; ++b) k.blocks.emplace_back((size_t)b * S, S);                 // U, V, W x 2 levels
+    if (nmx)
+        for (int b = 0; b < 18; ++b) k.blocks.emplace_back(nf + (size_t)b * (nmx / 18), nmx / 18);   // [side][var]
+    if (nmz)
+        for (int b = 0; b < 18; ++b) k.blocks.emplace_back(nf + nmx + (size_t)b * (nmz / 18), nmz / 18);
+    if (G <= 1) return;
+    const size_t es = codec == MNAD_SNAP_F16 ? 2 : 4;
+    k.data = DevMem(&ctx, (size_t)(G - 1) * k.slot * es);
+    if (codec == MNAD_SNAP_F16) {
+        k.scale = DevMem(&ctx, (size_t)(G - 1) * k.blocks.size() * sizeof(float));
+        k.maxbits = DevMem(&ctx, (size_t)(G - 1) * k.blocks.size() * sizeof(unsigned));
+    }
+}
+
+// The state arrays of a propagation in slot order: fields, mx, mz.
+static void state_parts(Prop& p, float* part[3], size_t count[3])
+{
+    part[0] = p.fields.as<float>(); count[0] = p.fields.size() / sizeof(float);
+    part[1] = p.mx.as<float>();     count[1] = p.mx.size() / sizeof(float);
+    part[2] = p.mz.as<float>();     count[2] = p.mz.size() / sizeof(float);
+}
+
+void Prop::save_state(Context& ctx, int g)
+{
+    Checkpoints& k = ckpt;
+    if (g < 1 || g >= k.G) return;
+    float* part[3];
+    size_t count[3];
+    state_parts(*this, part, count);
+    cudaStream_t st = ctx.stream;
+    if (k.codec == MNAD_SNAP_F32) {
+        float* dst = k.data.as<float>() + (size_t)(g - 1) * k.slot;
+        for (int a = 0; a < 3; ++a) {
+            if (count[a]) MNAD_CK(cudaMemcpyAsync(dst, part[a], count[a] * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            dst += count[a];
+        }
+        return;
+    }
+    const size_t nb = k.blocks.size();
+    unsigned* mb = k.maxbits.as<unsigned>() + (size_t)(g - 1) * nb;
+    float* sc = k.scale.as<float>() + (size_t)(g - 1) * nb;
+    __half* dst = k.data.as<__half>() + (size_t)(g - 1) * k.slot;
+    MNAD_CK(cudaMemsetAsync(mb, 0, nb * sizeof(unsigned), st));
+    // slot offsets map onto the three arrays in order
+    auto src_of = [&](size_t off) -> const float* {
+        for (int a = 0; a < 3; ++a) {
+            if (off < count[a]) return part[a] + off;
+            off -= count[a];
+        }
+        return nullptr;
+    };
+    for (size_t b = 0; b < nb; ++b) {
+        const size_t off = k.blocks[b].first, n = k.blocks[b].second;
+        const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)ctx.num_sms * 4);
+        f16_absmax<<<std::max(blocks, 1), 256, 0, st>>>(src_of(off), n, mb + b);
+        f16_encode<<<std::max(blocks, 1), 256, 0, st>>>(src_of(off), n, mb + b, dst + off, sc + b);
+    }
+    MNAD_CK(cudaGetLastError());
+}
+
+void Prop::restore_state(Context& ctx, int g)
+{
+    Checkpoints& k = ckpt;
+    cudaStream_t st = ctx.stream;
+    float* part[3];
+    size_t count[3];
+    state_parts(*this, part, count);
+    if (g <= 0) {
+        for (int a = 0; a < 3; ++a)
+            if (count[a]) MNAD_CK(cudaMemsetAsync(part[a], 0, count[a] * sizeof(float), st));
+        seed_sources<<<1, 32, 0, st>>>(d_desc.as<PropDesc>(), 1);
+        MNAD_CK(cudaGetLastError());
+        return;
+    }
+    if (g >= k.G) throw Error(MNAD_E_STATE, "no checkpoint " + std::to_string(g));
+    if (k.codec == MNAD_SNAP_F32) {
+        const float* src = k.data.as<float>() + (size_t)(g - 1) * k.slot;
+        for (int a = 0; a < 3; ++a) {
+            if (count[a]) MNAD_CK(cudaMemcpyAsync(part[a], src, count[a] * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            src += count[a];
+        }
+        return;
+    }
+    const size_t nb = k.blocks.size();
+    const float* sc = k.scale.as<float>() + (size_t)(g - 1) * nb;
+    const __half* src = k.data.as<__half>() + (size_t)(g - 1) * k.slot;
+    auto dst_of = [&](size_t off) -> float* {
+        for (int a = 0; a < 3; ++a) {
+            if (off < count[a]) return part[a] + off;
+            off -= count[a];
+        }
+        return nullptr;
+    };
+    for (size_t b = 0; b < nb; ++b) {
+        const size_t off = k.blocks[b].first, n = k.blocks[b].second;
+        const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)ctx.num_sms * 4);
+        f16_decode<<<std::max(blocks, 1), 256, 0, st>>>(src + off, n, sc + b, dst_of(off));
+    }
     MNAD_CK(cudaGetLastError());
 }
 
@@ -566,13 +685,43 @@ size_t Batch::reserve_counters(int nsteps)
     return need;
 }
 
+void Batch::checkpoint_after(int s)
+{
+    for (Prop* p : props_) {
+        const Checkpoints& k = p->ckpt;
+        if (!k.saving || k.C <= 0) continue;
+        const int sl = s - p->desc.s_off;
+        if (sl < 0 || sl + 1 > p->spec.nt || (sl + 1) % k.C != 0) continue;
+        p->save_state(ctx_, (sl + 1) / k.C);
+    }
+}
+
+void Batch::refresh_descs()
+{
+    std::vector<PropDesc> all;
+    for (auto& g : groups_) {
+        std::vector<PropDesc> descs;
+        int base = 0;
+        for (Prop* p : g->props) {
+            PropDesc D = p->desc;
+            D.tile_base = base;                 // this batch's tile numbering
+            base += D.ntz * D.ntx;
+            descs.push_back(D);
+            all.push_back(D);
+        }
+        if (!descs.empty()) upload(ctx_, g->desc.get(), descs.data(), descs.size() * sizeof(PropDesc));
+    }
+    if (!all.empty()) upload(ctx_, d_all_desc_.get(), all.data(), all.size() * sizeof(PropDesc));
+}
+
 void Batch::advance(int s0, int s1)
 {
     if (ntiles_ == 0) return;
-    bool f16 = false, en = false;
+    bool f16 = false, en = false, ck = false;
     for (Prop* p : props_) {
         f16 |= p->spec.mode == MODE_FWD && p->spec.wf && p->spec.wf->codec == MNAD_SNAP_F16;
         en |= p->energy.get() != nullptr;
+        ck |= p->ckpt.saving && p->ckpt.C > 0;
     }
     if (tc_.kind == MNAD_KERNEL_TMA && s1 > s0) {
         // one tile counter per step and group, zeroed before these launches
@@ -583,6 +732,7 @@ void Batch::advance(int s0, int s1)
         launch_step(s, s - s0);
         if (f16) encode_snapshots(s);
         if (en) energy_after(s);
+        if (ck) checkpoint_after(s);
     }
     MNAD_CK(cudaGetLastError());
 }

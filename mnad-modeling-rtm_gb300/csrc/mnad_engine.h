@@ -49,6 +49,7 @@ private:
 // UU_<ss>.mat / illum_<ss>.mat pair), resident on the device.
 struct Wavefield {
     int nz = 0, nx = 0, d = 0, nt = 0, T = 0, nsnap = 0, ncols = 0, codec = 0;
+    int held = 0;             // snapshot columns allocated: nsnap, or a segment of a checkpointed run
     size_t nint = 0;
     DevMem snap, scale, illum;
     DevMem stage, maxbits;   // FP16 codec: FP32 staging snapshot, per-snapshot max |d2u|
@@ -97,6 +98,17 @@ struct PropSpec {
     int energy_every = 0;              // forward: FP64 energy every that many steps
 };
 
+// Saved states of a forward propagation (checkpointed RTM).  Slot g - 1
+// holds the state (both time levels of U, V, W and the CPML memory variables)
+// after g*C steps, g = 1 .. G-1; the state after 0 steps is a fresh start.
+struct Checkpoints {
+    int C = 0, G = 0, codec = MNAD_SNAP_F32;
+    bool saving = false;                  // save while the propagation runs
+    size_t slot = 0;                      // elements per slot (fields, then mx, then mz)
+    std::vector<std::pair<size_t, size_t>> blocks;   // FP16: (offset, count) of each scaled array
+    DevMem data, scale, maxbits;          // data [G-1][slot]; FP16: scale, maxbits [G-1][blocks]
+};
+
 // Device state of one propagation.
 struct Prop {
     PropSpec spec;
@@ -110,6 +122,10 @@ struct Prop {
     void build(Context& ctx, const TileCfg& tc);
     void reset(Context& ctx);          // zero the state of a fresh run (stream-ordered)
     void start(Context& ctx, int s_off);   // reset + seed the source; run from global step s_off (even)
+    Checkpoints ckpt;
+    void setup_checkpoints(Context& ctx, int C, int G, int codec);
+    void save_state(Context& ctx, int g);       // state after g*C steps into slot g-1 (async)
+    void restore_state(Context& ctx, int g);    // g = 0: fresh start (zero state, source seeded)
     size_t nint() const { return (size_t)(spec.nz - 2 * spec.d) * (spec.nx - 2 * spec.d); }
     double point_updates() const { return (double)spec.nz * spec.nx * spec.nt; }
     double algorithmic_bytes() const;
@@ -136,6 +152,7 @@ public:
     void run(bool use_graph);          // start() + every step, optionally as one CUDA graph (async)
     void start();                      // zero all state and seed the sources (async)
     void advance(int s0, int s1);      // launch global steps s0..s1-1 (async)
+    void refresh_descs();              // re-upload the descriptors after host-side changes
     int steps() const { return nsteps_; }
     int tiles() const { return ntiles_; }
     const std::vector<Prop*>& props() const { return props_; }
@@ -144,6 +161,7 @@ private:
     size_t reserve_counters(int nsteps);   // tile counters for nsteps steps (bytes used)
     void encode_snapshots(int s);      // FP16 codec: encode the snapshots taken at step s
     void energy_after(int s);          // energy diagnostic after step s
+    void checkpoint_after(int s);      // checkpointed propagations: save the state after step s
     Context& ctx_;
     TileCfg tc_;
     std::vector<Prop*> props_;

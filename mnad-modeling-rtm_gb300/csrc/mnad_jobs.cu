@@ -44,14 +44,15 @@ void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, 
 }
 
 std::unique_ptr<Wavefield> new_wavefield(Context& c, int nz, int nx, int d, int nt, int T, int ncols,
-                                                int nsnap, int codec)
+                                                int nsnap, int codec, int held)
 {
     auto wf = std::make_unique<Wavefield>();
     wf->nz = nz; wf->nx = nx; wf->d = d; wf->nt = nt; wf->T = T;
     wf->ncols = ncols; wf->nsnap = nsnap; wf->codec = codec;
+    wf->held = held < 0 ? nsnap : held;
     wf->nint = (size_t)(nz - 2 * d) * (nx - 2 * d);
     const size_t cb = codec == MNAD_SNAP_F32 ? 4 : 2;
-    wf->snap = DevMem(&c, std::max<size_t>(1, wf->nint * (size_t)nsnap * cb));
+    wf->snap = DevMem(&c, std::max<size_t>(1, wf->nint * (size_t)wf->held * cb));
     wf->illum = DevMem(&c, std::max<size_t>(1, wf->nint * sizeof(double)));
     MNAD_CK(cudaMemsetAsync(wf->illum.get(), 0, wf->illum.size(), c.stream));
     if (codec == MNAD_SNAP_F16) {

@@ -37,8 +37,9 @@ int index1(double x, int n, const char* what);
 void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, const double* v);
 void check_job(const mnad_job& j, int k);
 void fill_receivers(PropSpec& s, const double* xr, const double* zr, int nr);
+// `held` snapshot columns are allocated (< 0: all nsnap).
 std::unique_ptr<Wavefield> new_wavefield(Context& c, int nz, int nx, int d, int nt, int T, int ncols, int nsnap,
-                                         int codec);
+                                         int codec, int held = -1);
 // Snapshot interval of an RTM job (job.T or the reference formula on vs)
 // and the UU column count max(2 nf + 1, floor(nt/T)).
 void rtm_snapshot_plan(const mnad_job& j, int& T, int& ncols);

@@ -155,17 +155,27 @@ __global__ void f16_absmax(const float* __restrict__ x, size_t n, unsigned* __re
 
 // FP16 encoding of one snapshot with a power-of-two scale s chosen from its
 // maximum so that max/s < 2^14 (no saturation; the scale multiply is exact).
+// Arrays whose maximum is below 2^-100 keep s = 2^-114, so 1/s stays finite.
 __global__ void f16_encode(const float* __restrict__ x, size_t n, const unsigned* __restrict__ maxbits,
                            __half* __restrict__ out, float* __restrict__ scale)
 {
     const float mx = __uint_as_float(*maxbits);
     int e = 0;
     frexpf(mx, &e);                                   // mx = f * 2^e, 0.5 <= f < 1
+    e = max(e, -100);                                 // tiny maxima: keep 2^(14-e) finite
     const float s = mx > 0.0f ? ldexpf(1.0f, e - 14) : 1.0f;
     const float inv = mx > 0.0f ? ldexpf(1.0f, 14 - e) : 1.0f;
     if (blockIdx.x == 0 && threadIdx.x == 0) *scale = s;
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
         out[k] = __float2half_rn(x[k] * inv);
+}
+
+__global__ void f16_decode(const __half* __restrict__ in, size_t n, const float* __restrict__ scale,
+                           float* __restrict__ out)
+{
+    const float s = *scale;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        out[k] = __half2float(in[k]) * s;
 }
 
 // Energy of one propagation after a step, in FP64 over the image region:

@@ -42,6 +42,9 @@ __global__ void scale_f64(const double* __restrict__ in, double s, size_t n, dou
 __global__ void f16_absmax(const float* __restrict__ x, size_t n, unsigned* __restrict__ maxbits);
 __global__ void f16_encode(const float* __restrict__ x, size_t n, const unsigned* __restrict__ maxbits,
                            __half* __restrict__ out, float* __restrict__ scale);
+// FP16 -> FP32 of one array stored by f16_encode (value * scale).
+__global__ void f16_decode(const __half* __restrict__ in, size_t n, const float* __restrict__ scale,
+                           float* __restrict__ out);
 __global__ void energy_reduce(const PropDesc* __restrict__ desc, int lvl_new, double* __restrict__ out);
 __global__ void axpy_f64(double a, const double* __restrict__ x, size_t n, double* __restrict__ y);
 __global__ void divide_f64(const double* __restrict__ num, const double* __restrict__ den, size_t n,

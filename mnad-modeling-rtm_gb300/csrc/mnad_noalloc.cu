@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -136,6 +137,7 @@ void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, doub
 
     PropDesc D;
     std::memset(&D, 0, sizeof(D));
+    D.s_begin = INT_MIN; D.s_end = INT_MAX;
     D.mode = MODE_FWD; D.nt = nt; D.nz = nz; D.nx = nx; D.ld = ld; D.d = d; D.dpz = dpz; D.zb0 = (nz - d) & ~3;
     D.ntz = ntz; D.ntx = ntx; D.tile_base = 0;
     for (int t = 0; t < 2; ++t)

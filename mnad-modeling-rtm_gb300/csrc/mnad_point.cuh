@@ -17,11 +17,12 @@ __device__ __forceinline__ void load_desc(PropDesc& dst, const PropDesc* src)
 }
 
 // Current time index of a propagation at global step s (1-based tt), or 0
-// when it has no work at this step.
-// The local step is s - s_off; s_off is even, so the time level s & 1 is the
-// same for every propagation of a launch.
+// when it has no work at this step (outside its window [s_begin, s_end) or
+// its nt steps).  The local step is s - s_off; s_off is even, so the time
+// level s & 1 is the same for every propagation of a launch.
 __device__ __forceinline__ int step_tt(const PropDesc& P, int s)
 {
+    if (s < P.s_begin || s >= P.s_end) return 0;
     s -= P.s_off;
     if (s < 0 || s >= P.nt) return 0;
     return P.mode == MODE_FWD ? s + 1 : P.nt - s;
@@ -130,10 +131,13 @@ __device__ __forceinline__ void finish_point(const PropDesc& P, int tt, int j, i
             d2u *= P.inv_dt2;
             const size_t q = (size_t)(j - d) + (size_t)(i - d) * niz;
             const size_t nint = (size_t)niz * (P.nx - 2 * d);
-            const size_t o = (P.snap_stage ? (size_t)0 : (size_t)(tt / P.T - 1)) * nint + q;
-            if (P.codec == CODEC_BF16) static_cast<__nv_bfloat16*>(P.snap)[o] = __float2bfloat16_rn(d2u);
-            else static_cast<float*>(P.snap)[o] = d2u;   // FP32, or the FP16 codec's staging slot
-            P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
+            const int slot = P.snap_stage ? 0 : tt / P.T - 1 - P.snap_col0;
+            if ((P.snap_flags & SNAP_WRITE) && slot >= 0 && slot < P.snap_cols) {
+                const size_t o = (size_t)slot * nint + q;
+                if (P.codec == CODEC_BF16) static_cast<__nv_bfloat16*>(P.snap)[o] = __float2bfloat16_rn(d2u);
+                else static_cast<float*>(P.snap)[o] = d2u;   // FP32, or the FP16 codec's staging slot
+            }
+            if (P.snap_flags & SNAP_ILLUM) P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
         }
         if ((long long)p == P.src && tt < P.nt) xu += P.src_amp[tt];   // next step's injection
     } else {
@@ -144,11 +148,12 @@ __device__ __forceinline__ void finish_point(const PropDesc& P, int tt, int j, i
             // Born_adj_MNAD.m:127-134: pairs column ncols-ttt+1 of UU.
             const int ttt = P.img_steps - tt / P.T;              // 0-based imaging count
             const int col = (P.pairing == PAIR_REFERENCE ? P.ncols : P.nsnap) - ttt;   // 1-based
-            if (col >= 1 && col <= P.nsnap) {
+            const int slot = col - 1 - P.snap_col0;
+            if (col >= 1 && col <= P.nsnap && slot >= 0 && slot < P.snap_cols) {
                 const size_t q = (size_t)(j - d) + (size_t)(i - d) * niz;
                 const size_t nint = (size_t)niz * (P.nx - 2 * d);
                 const float sc = P.codec == CODEC_F16 ? P.snap_scale[col - 1] : 1.0f;
-                const float us = snap_decode(P.snap, P.codec, (size_t)(col - 1) * nint + q, sc);
+                const float us = snap_decode(P.snap, P.codec, (size_t)slot * nint + q, sc);
                 P.image[q] = fma((double)us, (double)xu, P.image[q]);
             }
         }

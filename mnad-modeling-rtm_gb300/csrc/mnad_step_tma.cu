@@ -594,7 +594,7 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
             int col = 0;
             if (mode == MODE_ADJ && snap_step) {
                 col = (P.pairing == PAIR_REFERENCE ? P.ncols : P.nsnap) - (P.img_steps - tq);
-                if (col < 1 || col > P.nsnap) col = 0;
+                if (col < 1 || col > P.nsnap || col - 1 < P.snap_col0 || col - 1 - P.snap_col0 >= P.snap_cols) col = 0;
             }
             const int src = P.src;
             const float src_next = (has_src && mode == MODE_FWD && src >= p && src < p + Q && tt < nt)
@@ -650,10 +650,14 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                         else if (tt == 2) d2u = su[k] - pu[k];
                         d2u *= P.inv_dt2;
                         const size_t q = (size_t)(q0 + k);
-                        const size_t o = (P.snap_stage ? (size_t)0 : (size_t)(tq - 1)) * nint + q;
-                        if (P.codec == CODEC_BF16) static_cast<__nv_bfloat16*>(P.snap)[o] = __float2bfloat16_rn(d2u);
-                        else static_cast<float*>(P.snap)[o] = d2u;
-                        P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
+                        const int slot = P.snap_stage ? 0 : tq - 1 - P.snap_col0;
+                        if ((P.snap_flags & SNAP_WRITE) && slot >= 0 && slot < P.snap_cols) {
+                            const size_t o = (size_t)slot * nint + q;
+                            if (P.codec == CODEC_BF16)
+                                static_cast<__nv_bfloat16*>(P.snap)[o] = __float2bfloat16_rn(d2u);
+                            else static_cast<float*>(P.snap)[o] = d2u;
+                        }
+                        if (P.snap_flags & SNAP_ILLUM) P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
                     }
                 }
                 if (src_next != 0.0f) {
@@ -677,7 +681,7 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                         if (!(jk >= d && jk < nz - d && i >= d && i < nx - d)) continue;
                         const size_t q = (size_t)(q0 + k);
                         const float sc = P.codec == CODEC_F16 ? P.snap_scale[col - 1] : 1.0f;
-                        const float us = snap_decode(P.snap, P.codec, (size_t)(col - 1) * nint + q, sc);
+                        const float us = snap_decode(P.snap, P.codec, (size_t)(col - 1 - P.snap_col0) * nint + q, sc);
                         P.image[q] = fma((double)us, (double)ou[k], P.image[q]);
                     }
                 }

@@ -31,7 +31,7 @@ _vp = C.c_void_p
 class Options(C.Structure):
     _fields_ = [("snapshot_codec", C.c_int), ("pairing", C.c_int), ("T", C.c_int),
                 ("record_vw", C.c_int), ("use_graphs", C.c_int), ("kernel", C.c_int),
-                ("energy_every", C.c_int)]
+                ("energy_every", C.c_int), ("checkpoint_every", C.c_int), ("checkpoint_codec", C.c_int)]
 
 
 class Job(C.Structure):

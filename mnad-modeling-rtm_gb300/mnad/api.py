@@ -72,10 +72,11 @@ class Context:
         inv = lambda d, v: next(k for k, x in d.items() if x == v)
         return {"snapshot_codec": inv(_CODECS, o.snapshot_codec), "pairing": inv(_PAIRINGS, o.pairing),
                 "T": o.T, "record_vw": bool(o.record_vw), "use_graphs": bool(o.use_graphs),
-                "kernel": inv(_KERNELS, o.kernel), "energy_every": o.energy_every}
+                "kernel": inv(_KERNELS, o.kernel), "energy_every": o.energy_every,
+                "checkpoint_every": o.checkpoint_every, "checkpoint_codec": inv(_CODECS, o.checkpoint_codec)}
 
     def set_options(self, snapshot_codec=None, pairing=None, T=None, record_vw=None, use_graphs=None,
-                    kernel=None, energy_every=None):
+                    kernel=None, energy_every=None, checkpoint_every=None, checkpoint_codec=None):
         o = Options()
         check(lib().mnad_context_get_options(self._h, C.byref(o)))
         if snapshot_codec is not None:
@@ -92,6 +93,10 @@ class Context:
             o.kernel = _KERNELS[kernel]
         if energy_every is not None:
             o.energy_every = int(energy_every)
+        if checkpoint_every is not None:
+            o.checkpoint_every = int(checkpoint_every)
+        if checkpoint_codec is not None:
+            o.checkpoint_codec = _CODECS[checkpoint_codec]
         check(lib().mnad_context_set_options(self._h, C.byref(o)))
 
     def memory(self) -> int:
