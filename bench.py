@@ -48,8 +48,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--shots", type=int, default=64)
-    ap.add_argument("--nt", type=int, default=4000)
+    ap.add_argument("--workload", default="config3", choices=["config3", "config5"],
+                    help="config3: batched RTM (default); config5: large-grid RTM with FP16 checkpoints")
+    ap.add_argument("--shots", type=int, default=None, help="shots per pass (config3: 64, config5: 16)")
+    ap.add_argument("--nt", type=int, default=None, help="record length in steps (config3: 4000, config5: 6000)")
+    ap.add_argument("--checkpoint-every", type=int, default=360, help="config5: checkpoint interval (steps)")
     ap.add_argument("--plain-shots", type=int, default=2)
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, plain and CPU legs")
     ap.add_argument("--ref-steps", type=int, default=12, help="reference arm: time steps per worker sample")
@@ -278,10 +281,23 @@ def run_ours(args):
     rank, world, local = dist_setup(args.gpus)
     import mnad
     from mnad import workflow
-    sv = workflow.config3(seed=rank, nshots=args.shots, nt=args.nt)
+    if args.workload == "config5":
+        sv = workflow.config5(seed=0, nshots=256, nt=args.nt, first=rank * args.shots, count=args.shots)
+        ctx = mnad.Context(local, kernel=args.kernel, checkpoint_every=args.checkpoint_every, checkpoint_codec="f16")
+        data_desc = "synthetic (seeded faulted layered model with a salt body)"
+        wl = {"workload": "large-grid RTM with checkpoint-and-recompute, config 5",
+              "grid": "1201x4001 (+2x40 CPML) @ 12.5 m", "checkpoints": f"f16 every {args.checkpoint_every} steps",
+              "snapshot_buffer": "f32 segment", "propagations_per_shot": "3 + 1 recomputed background forward"}
+    else:
+        sv = workflow.config3(seed=rank, nshots=args.shots, nt=args.nt)
+        ctx = mnad.Context(local, snapshot_codec=sv.codec, kernel=args.kernel)
+        data_desc = "synthetic (seeded Gaussian random field + dipping reflectors)"
+        wl = {"workload": "batched RTM, config 3", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
+              "snapshots": sv.codec, "propagations_per_shot": 3}
     jobs = workflow.shot_jobs(sv, "rtm")
-    ctx = mnad.Context(local, snapshot_codec=sv.codec, kernel=args.kernel)
+    m0 = ctx.memory()
     plan = ctx.plan(jobs)
+    mem_per_shot = (ctx.memory() - m0) / max(len(jobs), 1)
     for _ in range(max(args.warmup, 0)):
         plan.run()
     barrier_sync(world)
@@ -310,7 +326,7 @@ def run_ours(args):
     achieved = abytes * args.steps / (sum(step_ms) / 1e3) / 1e9
     tr = profile_traffic()
     traffic = None
-    if tr and "bytes_per_point_update" in tr:
+    if tr and "bytes_per_point_update" in tr and args.workload == "config3":
         traffic = tr["bytes_per_point_update"] * pts / (plan.timing()["step_launches"])
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -359,17 +375,17 @@ def run_ours(args):
         if rank == 0:
             extras["cpu_baseline"] = cpu_baseline(sv)
     ctx.close()
-    if rank == 0 and args.serve_jobs > 0 and not args.no_extras:
+    if rank == 0 and args.serve_jobs > 0 and not args.no_extras and args.workload == "config3":
         extras["serving"] = serving_leg(local, args.serve_jobs, args.serve_rate, kernel=args.kernel)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Gpts/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 2),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded Gaussian random field + dipping reflectors)",
-                "config": {"workload": "batched RTM, config 3", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
-                           "shots": len(jobs), "nt": sv.nt, "dt": sv.dt, "propagations_per_shot": 3,
-                           "snapshots": sv.codec, "image": "f64", "parallelism": f"replicas x{world}",
-                           "l2": "state per step >> L2 (inputs larger than L2)"},
+                "data": data_desc,
+                "config": dict(wl, shots=len(jobs), nt=sv.nt, dt=sv.dt, image="f64",
+                               parallelism=f"replicas x{world}",
+                               l2="state per step >> L2 (inputs larger than L2)",
+                               device_bytes_per_shot=int(mem_per_shot)),
                 "shots_per_hr": round(shots_hr, 1), "roofline": roof, "clocks": clocks,
                 "gpu_launches": launches, "wall_s": round(wall, 2), "device_status": status}
         line.update(extras)
@@ -441,6 +457,10 @@ def run_reference(args):
 
 if __name__ == "__main__":
     a = parse()
+    if a.shots is None:
+        a.shots = 16 if a.workload == "config5" else 64
+    if a.nt is None:
+        a.nt = 6000 if a.workload == "config5" else 4000
     if a.impl == "reference":
         run_reference(a)
     else:

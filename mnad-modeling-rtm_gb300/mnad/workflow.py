@@ -151,6 +151,57 @@ def config3(seed: int = 0, nshots: int = 64, nt: int = 4000, codec: str = "bf16"
     return Survey("config3", pad_model(V, d), h, h, 1e-3, nt, d, 20.0, shots, vs=pad_model(Vs, d), codec=codec)
 
 
+def faulted_model(nz: int, nx: int, h: float, rng, nfaults: int = 6) -> np.ndarray:
+    """Seeded faulted sedimentary model: 10-16 layers whose velocities rise
+    with depth from 1500 to about 4000 m/s (gently undulating interfaces),
+    ``nfaults`` normal faults (60-70 degree dip, 40-200 m throw, hanging wall
+    down) and a salt-like 4500 m/s body; clipped to 1500-4500 m/s."""
+    z = np.arange(nz, dtype=np.float64)[:, None] * h
+    x = np.arange(nx, dtype=np.float64)[None, :] * h
+    zmax, xmax = nz * h, nx * h
+    # depth in the layer frame: faults shift the hanging wall down by the throw
+    zl = np.broadcast_to(z, (nz, nx)).copy()
+    for _ in range(nfaults):
+        x0 = rng.uniform(0.1, 0.9) * xmax
+        dip = np.deg2rad(rng.uniform(60.0, 70.0)) * rng.choice((-1.0, 1.0))
+        throw = rng.uniform(40.0, 200.0)
+        hanging = (x - x0) * np.sign(dip) > (z / np.tan(abs(dip)))
+        zl -= throw * hanging
+    nl = int(rng.integers(10, 17))
+    tops = np.sort(rng.uniform(0.03, 0.95, nl - 1)) * zmax
+    vel = np.sort(rng.uniform(1500.0, 4000.0, nl))
+    vel[0] = 1500.0
+    und = 0.01 * zmax * np.sin(2 * np.pi * x / rng.uniform(0.2, 0.6) / xmax + rng.uniform(0, 2 * np.pi))
+    V = vel[np.searchsorted(tops, zl + und, side="right")]
+    # salt body: an ellipse with a rough top
+    cz, cx = rng.uniform(0.45, 0.7) * zmax, rng.uniform(0.3, 0.7) * xmax
+    az, ax = rng.uniform(0.08, 0.15) * zmax, rng.uniform(0.06, 0.12) * xmax
+    rough = 1.0 + 0.15 * np.sin(5 * np.pi * x / xmax + rng.uniform(0, 2 * np.pi))
+    V = np.where(((z - cz) / (az * rough)) ** 2 + ((x - cx) / ax) ** 2 < 1.0, 4500.0, V)
+    return np.clip(V, 1500.0, 4500.0)
+
+
+def config5(seed: int = 0, nshots: int = 256, nt: int = 6000, first: int = 0, count: Optional[int] = None) -> Survey:
+    """Large-scale RTM at 2 points per minimum wavelength: 1201 (z) x 4001 (x)
+    at 12.5 m (1281 x 4081 padded), vmin 1500 m/s; seeded faulted
+    sedimentary model with a 4500 m/s salt body; ``nshots`` shots spread over
+    the line, receivers on every column at 25 m depth; 25 Hz Ricker; dt =
+    1 ms; 6 s; migration model = 15-point Gaussian smoothing.  ``first`` /
+    ``count`` select a subset of the shots (same model)."""
+    rng = np.random.default_rng(seed)
+    nzp, nxp, h, d = 1201, 4001, 12.5, 40
+    V = faulted_model(nzp, nxp, h, rng)
+    Vs = gaussian_smooth(V, 15)
+    step = (nxp - 1) / max(nshots, 1)
+    count = nshots - first if count is None else count
+    shots = []
+    for s in range(first, first + count):
+        xg = int(round(step * (s + 0.5))) + 1
+        shots.append(Shot(d + 1, d + xg, np.full(nxp, d + 2), d + np.arange(1, nxp + 1)))
+    return Survey("config5", pad_model(V, d), h, h, 1e-3, nt, d, 25.0, shots, vs=pad_model(Vs, d), codec="f32",
+                  meta={"nshots_total": nshots})
+
+
 def shot_jobs(sv: Survey, kind: str = "rtm", shots=None, keep_data: bool = False):
     """mnad.api.ShotJob list for a survey (RTM: true + migration model)."""
     from .api import ShotJob
