@@ -280,7 +280,7 @@ def run_ours(args):
     import numpy as np
     rank, world, local = dist_setup(args.gpus)
     import mnad
-    from mnad import workflow
+    from mnad import shards, workflow
     if args.workload == "config5":
         sv = workflow.config5(seed=0, nshots=256, nt=args.nt, first=rank * args.shots, count=args.shots)
         ctx = mnad.Context(local, kernel=args.kernel, checkpoint_every=args.checkpoint_every, checkpoint_codec="f16")
@@ -289,7 +289,9 @@ def run_ours(args):
               "grid": "1201x4001 (+2x40 CPML) @ 12.5 m", "checkpoints": f"f16 every {args.checkpoint_every} steps",
               "snapshot_buffer": "f32 segment", "propagations_per_shot": "3 + 1 recomputed background forward"}
     else:
-        sv = workflow.config3(seed=rank, nshots=args.shots, nt=args.nt)
+        # weak scaling: every rank images args.shots shots of one survey
+        sv = workflow.config3(seed=0, nshots=args.shots * world, nt=args.nt)
+        sv.shots = shards.shard(sv.shots, rank, world)
         ctx = mnad.Context(local, snapshot_codec=sv.codec, kernel=args.kernel)
         data_desc = "synthetic (seeded Gaussian random field + dipping reflectors)"
         wl = {"workload": "batched RTM, config 3", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
@@ -333,8 +335,15 @@ def run_ours(args):
             "peak_kind": f"{peak_kind} hbm_gbs",
             "kernel": "mnad::step_direct" if args.kernel == "direct" else "mnad::step_tma",
             "algorithmic_bytes_per_launch": abytes / plan.timing()["step_launches"]}
+    # the one exchange of the path: the FP64 image / illumination stack over ranks
+    t = time.perf_counter()
+    im, il, _ = plan.stack()
+    if world > 1:
+        im, il, _ = shards.reduce_stack(im, il)
+    stack = {"shots_total": int(allsum(len(jobs), world)), "reduce_ms": round((time.perf_counter() - t) * 1e3, 2),
+             "image_norm": float(np.linalg.norm(im))}
     plan.close()
-    extras = {}
+    extras = {"stack": stack}
     if not args.no_extras:
         # e2e through the C ABI with host buffers in pinned memory (upload, run,
         # download inside the timed region)

@@ -142,7 +142,9 @@ def config3(seed: int = 0, nshots: int = 64, nt: int = 4000, codec: str = "bf16"
         band = np.abs(z - (z0 + dip * (x - x.mean()))) < 1.5 * h
         V = V + 400.0 * band
     Vs = gaussian_smooth(V, 15)
-    spacing = int(round(187.5 / h))
+    # 187.5 m apart; a longer shot list (shards of a multi-GPU run) is spread
+    # evenly over the line instead
+    spacing = max(1, min(int(round(187.5 / h)), (nxp - 1) // max(nshots, 1)))
     first = (nxp - spacing * (nshots - 1)) // 2
     shots = []
     for s in range(nshots):
