@@ -386,6 +386,10 @@ def run_ours(args):
     ctx.close()
     if rank == 0 and args.serve_jobs > 0 and not args.no_extras and args.workload == "config3":
         extras["serving"] = serving_leg(local, args.serve_jobs, args.serve_rate, kernel=args.kernel)
+        # the same stream all at once: the server's capacity (latency is then queueing)
+        cap = serving_leg(local, args.serve_jobs, 1e6, kernel=args.kernel)
+        extras["serving"]["capacity"] = {k: cap[k] for k in ("value", "unit", "jobs_per_s", "rtm_jobs_per_hr",
+                                                            "p50_ms", "p99_ms", "wall_s", "failed")}
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Gpts/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 2),

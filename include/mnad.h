@@ -253,6 +253,10 @@ typedef struct mnad_server_options {
     int max_active_jobs;      /* <= 0: limited by the budget only */
     int snapshot_codec;       /* MNAD_SNAP_* of RTM snapshots */
     int kernel;               /* MNAD_KERNEL_* */
+    int no_graphs;            /* 1: launch each tick's steps one by one instead of
+                                 replaying a CUDA graph of the tick (the graph is
+                                 captured again whenever the set of propagations
+                                 changes; FP16 snapshots never use it) */
 } mnad_server_options;
 
 enum { MNAD_JOB_QUEUED = 0, MNAD_JOB_RUNNING = 1, MNAD_JOB_DONE = 2, MNAD_JOB_FAILED = 3 };

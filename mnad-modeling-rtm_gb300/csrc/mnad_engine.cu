@@ -528,6 +528,7 @@ double Prop::algorithmic_bytes() const
 Batch::~Batch()
 {
     if (graph_) cudaGraphExecDestroy(graph_);
+    if (tick_graph_) cudaGraphExecDestroy(tick_graph_);
 }
 
 void Batch::finalize()
@@ -735,6 +736,39 @@ void Batch::advance(int s0, int s1)
         if (ck) checkpoint_after(s);
     }
     MNAD_CK(cudaGetLastError());
+}
+
+bool Batch::has_step_hooks() const
+{
+    for (const Prop* p : props_) {
+        if (p->spec.mode == MODE_FWD && p->spec.wf && p->spec.wf->codec == MNAD_SNAP_F16) return true;
+        if (p->energy.get() || (p->ckpt.saving && p->ckpt.C > 0)) return true;
+    }
+    return false;
+}
+
+void Batch::tick(int K, bool use_graph)
+{
+    if (ntiles_ == 0 || K <= 0) return;
+    if (!use_graph || has_step_hooks()) {
+        advance(0, K);
+        return;
+    }
+    if (!tick_graph_ || tick_K_ != K) {
+        if (tick_graph_) cudaGraphExecDestroy(tick_graph_);
+        tick_graph_ = nullptr;
+        if (tc_.kind == MNAD_KERNEL_TMA) reserve_counters(K);   // allocate outside the capture
+        cudaGraph_t g = nullptr;
+        MNAD_CK(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal));
+        advance(0, K);
+        cudaError_t e = cudaStreamEndCapture(ctx_.stream, &g);
+        MNAD_CK(e);
+        e = cudaGraphInstantiate(&tick_graph_, g, 0);
+        cudaGraphDestroy(g);
+        MNAD_CK(e);
+        tick_K_ = K;
+    }
+    MNAD_CK(cudaGraphLaunch(tick_graph_, ctx_.stream));
 }
 
 void Batch::run(bool use_graph)

@@ -153,6 +153,11 @@ public:
     void start();                      // zero all state and seed the sources (async)
     void advance(int s0, int s1);      // launch global steps s0..s1-1 (async)
     void refresh_descs();              // re-upload the descriptors after host-side changes
+    // Global steps 0..K-1 (async), as one CUDA graph replayed tick after tick
+    // when `use_graph` and no propagation needs per-step host work; callers
+    // shift each propagation's s_off by -K between ticks.
+    void tick(int K, bool use_graph);
+    bool has_step_hooks() const;       // FP16 snapshot encodes, energy or checkpoints per step
     int steps() const { return nsteps_; }
     int tiles() const { return ntiles_; }
     const std::vector<Prop*>& props() const { return props_; }
@@ -170,6 +175,8 @@ private:
     DevMem d_counters_;                // per step and group: tiles claimed (TMA kernel)
     int ntiles_ = 0, nsteps_ = 0;
     cudaGraphExec_t graph_ = nullptr;
+    cudaGraphExec_t tick_graph_ = nullptr;
+    int tick_K_ = 0;
 };
 
 // r = v^2 dt^2 (forward) or (v dt)^2 (adjoint) of a host model, in padded

@@ -78,7 +78,8 @@ struct mnad_server {
     size_t budget = 0, reserve = 0;          // HBM budget; part kept for batch tables
     std::atomic<size_t> mem_in_use{0};       // the context's device bytes, for other threads
     bool dirty = true;
-    int G = 0;                               // global step counter (even at tick boundaries)
+    // Each tick runs global steps 0..K-1; a propagation's local step at tick
+    // step s is s - s_off, and s_off drops by K after every tick.
     // statistics (under mu)
     int64_t n_submitted = 0, n_done = 0, n_failed = 0;
     std::vector<double> latencies_ms;
@@ -101,7 +102,7 @@ static void free_running_state(ServerJob* j)
 }
 
 // Admission: every propagation of the job is built (device state allocated)
-// and the forward propagations start at step G; the adjoint of an RTM job
+// and the forward propagations start at the next tick; the adjoint of an RTM job
 // starts when its forwards end.  Allocation stops short of the budget by a
 // reserve kept for the batch tables of the ticks.
 bool mnad_server::admit(ServerJob* j)
@@ -127,8 +128,8 @@ bool mnad_server::admit(ServerJob* j)
             j->points *= 3;
         }
         c.budget = budget;
-        j->fwd_true->start(c, G);
-        if (j->fwd_bg) j->fwd_bg->start(c, G);
+        j->fwd_true->start(c, 0);
+        if (j->fwd_bg) j->fwd_bg->start(c, 0);
         j->phase = 1;
         return true;
     } catch (const Error& e) {
@@ -191,7 +192,7 @@ void mnad_server::step_phase(ServerJob* j)
         c.sync();
         j->fwd_true.reset();
         j->fwd_bg.reset();                   // the snapshots stay in j->wf
-        j->adj->start(c, G);
+        j->adj->start(c, 0);
         j->phase = 2;
         return;
     }
@@ -260,14 +261,15 @@ void mnad_server::loop()
                 batch->finalize();
                 dirty = false;
             }
-            batch->advance(G, G + K);
-            G += K;
+            batch->refresh_descs();
+            batch->tick(K, opt.no_graphs == 0);
+            for (Prop* p : batch->props()) p->desc.s_off -= K;
             ctx->sync();
             // retire / advance the jobs whose current phase is over
             std::vector<ServerJob*> still;
             for (ServerJob* j : running) {
                 const Prop* p = j->phase == 2 ? j->adj.get() : j->fwd_true.get();
-                if (G - p->desc.s_off >= p->spec.nt) {
+                if (-p->desc.s_off >= p->spec.nt) {
                     step_phase(j);
                     dirty = true;
                 }

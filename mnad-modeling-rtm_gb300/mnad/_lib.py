@@ -44,7 +44,7 @@ class Job(C.Structure):
 
 class ServerOptions(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("chunk_steps", C.c_int), ("max_active_jobs", C.c_int),
-                ("snapshot_codec", C.c_int), ("kernel", C.c_int)]
+                ("snapshot_codec", C.c_int), ("kernel", C.c_int), ("no_graphs", C.c_int)]
 
 
 class ServerStats(C.Structure):

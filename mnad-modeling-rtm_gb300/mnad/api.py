@@ -339,8 +339,9 @@ class Server:
     """
 
     def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, chunk_steps: int = 64, max_active_jobs: int = 0,
-                 snapshot_codec: str = "f32", kernel: str = "auto"):
+                 snapshot_codec: str = "f32", kernel: str = "auto", graphs: bool = True):
         o = _lib.ServerOptions()
+        o.no_graphs = 0 if graphs else 1
         o.hbm_budget_bytes = int(hbm_budget_bytes)
         o.chunk_steps = int(chunk_steps)
         o.max_active_jobs = int(max_active_jobs)
