@@ -1,0 +1,75 @@
+"""Full-size parity of the benchmark configurations against the FP64 C
+oracle: config 2 (single-shot RTM, 381 x 681 padded, 3 s, T = 4) and one
+shot of config 3 (481 x 1281 padded, 4 s, snapshot interval by the reference
+formula) with FP32 and BF16 snapshots.  Each error is printed so the run log
+states it for every gather, snapshot set and image."""
+import numpy as np
+import pytest
+
+import mnad
+from mnad import workflow
+from oracle import coracle
+from oracle import mnad_oracle as P
+
+pytestmark = pytest.mark.gpu
+TOL_GATHER, TOL_IMAGE, TOL_BF16 = 1e-5, 1e-4, 1e-2
+
+
+def rel(a, b):
+    a, b = np.ravel(np.asarray(a), order="F"), np.ravel(np.asarray(b), order="F")
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from mnad import build
+    build.build()
+    with mnad.Context(0) as c:
+        yield c
+
+
+def _oracle_rtm(sv, sh, T):
+    nf = P.snapshot_nf(sv.vs, sv.nt)
+    T = T or P.snapshot_plan(sv.vs, sv.nt)[1]
+    ncols = max(2 * nf + 1, sv.nt // T)
+    a = (sv.dx, sh.xs, sh.xr, sv.dz, sh.zs, sh.zr)
+    data = coracle.fwd(*a, sv.v, sv.dt, sv.nt, sv.w, sv.d_pml)["datau"]
+    bg = coracle.fwd(*a, sv.vs, sv.dt, sv.nt, sv.w, sv.d_pml, indx=1, T=T, ncols=ncols)
+    im = coracle.adj(sv.dx, sv.dz, sv.nt, sv.dt, sv.vs, sh.xr, sh.zr, data - bg["datau"], sv.d_pml, bg["UU"], T)
+    return data, bg, im, T
+
+
+def _gpu_rtm(ctx, sv, sh, codec):
+    ctx.set_options(snapshot_codec=codec, T=sv.T)
+    try:
+        a = (sv.dx, sh.xs, sh.xr, sv.dz, sh.zs, sh.zr)
+        data = ctx.fwd(*a, sv.v, sv.dt, sv.nt, sv.w, sv.d_pml, ss=1)
+        datas = ctx.fwd(*a, sv.vs, sv.dt, sv.nt, sv.w, sv.d_pml, ss=1, indx=1)
+        UU, illum = ctx.wavefield_export(1)
+        im = ctx.adj(sv.dx, sv.dz, sv.nt, sv.dt, sv.vs, sh.xr, sh.zr, data - datas, sv.d_pml, ss=1)
+        ctx.wavefield_release(1)
+    finally:
+        ctx.set_options(snapshot_codec="f32", T=0)
+    return data, datas, UU, illum, im
+
+
+def _check(name, ctx, sv, shot, codecs):
+    data, bg, im_ref, T = _oracle_rtm(sv, shot, sv.T)
+    for codec in codecs:
+        d, ds, UU, illum, im = _gpu_rtm(ctx, sv, shot, codec)
+        errs = dict(gather=rel(d, data), gather_bg=rel(ds, bg["datau"]), snapshots=rel(UU, bg["UU"]),
+                    illum=rel(illum, bg["illum"]), image=rel(im, im_ref))
+        print(f"{name} T={T} {codec}: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+        assert errs["gather"] <= TOL_GATHER and errs["gather_bg"] <= TOL_GATHER
+        assert errs["illum"] <= TOL_IMAGE
+        assert errs["image"] <= (TOL_IMAGE if codec == "f32" else TOL_BF16)
+
+
+def test_config2_full_size(ctx):
+    sv = workflow.config2()
+    _check("config2", ctx, sv, sv.shots[0], ("f32", "bf16"))
+
+
+def test_config3_one_shot_full_size(ctx):
+    sv = workflow.config3(nshots=64)
+    _check("config3 shot 32", ctx, sv, sv.shots[32], ("f32", "bf16"))
