@@ -548,7 +548,9 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
         const bool snap_step = P.T > 0 && tt - tq * P.T == 0;
         // A plain tile (image region only, no source, no receivers, no
         // snapshot or imaging at this step) is stencil arithmetic and stores.
-        const bool plain = !(info.z & (TILE_STRIP | TILE_RECEIVERS | TILE_SOURCE)) && !snap_step;
+        // At snapshot / imaging steps (from tt = 3 on) a plain tile also stores its
+        // snapshot and illumination (forward) or adds its image term (adjoint).
+        const bool plain = !(info.z & (TILE_STRIP | TILE_RECEIVERS | TILE_SOURCE)) && (!snap_step || tt > 2);
         if (tt != 0 && plain) {
             constexpr int Q = TMA_PZ;
             float rr[Q];
@@ -579,6 +581,44 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
             *reinterpret_cast<float4*>(P.fld[cur ^ 1][0] + p) = make_float4(nu01.x, nu01.y, nu23.x, nu23.y);
             *reinterpret_cast<float4*>(P.fld[cur ^ 1][1] + p) = make_float4(nv01.x, nv01.y, nv23.x, nv23.y);
             *reinterpret_cast<float4*>(P.fld[cur ^ 1][2] + p) = make_float4(nw01.x, nw01.y, nw23.x, nw23.y);
+            if (snap_step) {
+                const int niz = nz - 2 * d;
+                const size_t nint = (size_t)niz * (nx - 2 * d);
+                const size_t q0 = (size_t)(j - d) + (size_t)(i - d) * niz;
+                if (mode == MODE_FWD) {
+                    // fwd_PDE_exact_MNAD.m:128-141 for tt > 2: d2u = nU - 2U + pU = su
+                    const float d2u[Q] = {su[0].x * P.inv_dt2, su[0].y * P.inv_dt2, su[1].x * P.inv_dt2,
+                                          su[1].y * P.inv_dt2};
+                    const int slot = P.snap_stage ? 0 : tq - 1 - P.snap_col0;
+                    if ((P.snap_flags & SNAP_WRITE) && slot >= 0 && slot < P.snap_cols) {
+                        const size_t o = (size_t)slot * nint + q0;
+#pragma unroll
+                        for (int k = 0; k < Q; ++k) {
+                            if (P.codec == CODEC_BF16)
+                                static_cast<__nv_bfloat16*>(P.snap)[o + k] = __float2bfloat16_rn(d2u[k]);
+                            else static_cast<float*>(P.snap)[o + k] = d2u[k];
+                        }
+                    }
+                    if (P.snap_flags & SNAP_ILLUM) {
+#pragma unroll
+                        for (int k = 0; k < Q; ++k)
+                            P.illum[q0 + k] = fma((double)d2u[k], (double)d2u[k], P.illum[q0 + k]);
+                    }
+                } else {
+                    // Born_adj_MNAD.m:127-134
+                    int col = (P.pairing == PAIR_REFERENCE ? P.ncols : P.nsnap) - (P.img_steps - tq);
+                    if (col >= 1 && col <= P.nsnap && col - 1 >= P.snap_col0 && col - 1 - P.snap_col0 < P.snap_cols) {
+                        const float sc = P.codec == CODEC_F16 ? P.snap_scale[col - 1] : 1.0f;
+                        const size_t o = (size_t)(col - 1 - P.snap_col0) * nint + q0;
+                        const float ou[Q] = {nu01.x, nu01.y, nu23.x, nu23.y};
+#pragma unroll
+                        for (int k = 0; k < Q; ++k) {
+                            const float us = snap_decode(P.snap, P.codec, o + k, sc);
+                            P.image[q0 + k] = fma((double)us, (double)ou[k], P.image[q0 + k]);
+                        }
+                    }
+                }
+            }
         } else if (tt != 0 && j < nz && i < nx) {
             constexpr int Q = TMA_PZ;
             float rr[Q];
