@@ -179,7 +179,8 @@ def cpu_baseline(sv, seconds=15.0):
     from oracle import coracle
     sh = sv.shots[0]
     w = sv.w
-    probe = 5
+    coracle.fwd(sv.dx, sh.xs, sh.xr, sv.dz, sh.zs, sh.zr, sv.v, sv.dt, 2, w, sv.d_pml)   # warm the thread pool
+    probe = 20
     t = time.perf_counter()
     coracle.fwd(sv.dx, sh.xs, sh.xr, sv.dz, sh.zs, sh.zr, sv.v, sv.dt, probe, w, sv.d_pml)
     per = (time.perf_counter() - t) / probe
