@@ -641,43 +641,45 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                                        ? P.src_amp[tt] : 0.0f;
             // lean: every point of the group inside the image region (no CPML, no edge)
             const bool lean = i >= d && i < nx - d && j >= d && j + Q - 1 < nz - d;
-            float su[Q], sv[Q], sw[Q];
+            float2 s2u[2], s2v[2], s2w[2];
             {
                 Window win;            // dies here: later phases re-read the stage
                 win.load(st, c, r0);
-                float2 s2u[2], s2v[2], s2w[2];
                 mnad_update_pairs(A.coef2, win, rr, s2u, s2v, s2w);
-                su[0] = s2u[0].x; su[1] = s2u[0].y; su[2] = s2u[1].x; su[3] = s2u[1].y;
-                sv[0] = s2v[0].x; sv[1] = s2v[0].y; sv[2] = s2v[1].x; sv[3] = s2v[1].y;
-                sw[0] = s2w[0].x; sw[1] = s2w[0].y; sw[2] = s2w[1].x; sw[3] = s2w[1].y;
             }
             if (!lean) {
                 float cu[Q], cv[Q], cw[Q];
 #pragma unroll
                 for (int k = 0; k < Q; ++k) cu[k] = cv[k] = cw[k] = 0.0f;
                 cpml_vec(P, st, c, r0, tt, j, i, p, has_src, rr, cu, cv, cw);
+                // sF -= r * (F1_x + F1_z), per point fmaf(-r, c, s)
 #pragma unroll
-                for (int k = 0; k < Q; ++k) {
-                    su[k] = fmaf(-rr[k], cu[k], su[k]);
-                    sv[k] = fmaf(-rr[k], cv[k], sv[k]);
-                    sw[k] = fmaf(-rr[k], cw[k], sw[k]);
+                for (int m = 0; m < 2; ++m) {
+                    const float2 nr = pr(-rr[2 * m], -rr[2 * m + 1]);
+                    s2u[m] = pfma(nr, pr(cu[2 * m], cu[2 * m + 1]), s2u[m]);
+                    s2v[m] = pfma(nr, pr(cv[2 * m], cv[2 * m + 1]), s2v[m]);
+                    s2w[m] = pfma(nr, pr(cw[2 * m], cw[2 * m + 1]), s2w[m]);
                 }
             }
-            float pu[Q], pv[Q], pw[Q], uc[Q], vc[Q], wc[Q];
-            ldv(&st.pts[0][txt][tzt * Q], pu);
-            ldv(&st.pts[1][txt][tzt * Q], pv);
-            ldv(&st.pts[2][txt][tzt * Q], pw);
-            ldv(&st.halo[0][c][r0], uc);
-            ldv(&st.halo[1][c][r0], vc);
-            ldv(&st.halo[2][c][r0], wc);
-            float ou[Q], ov[Q], ow[Q];
-#pragma unroll
-            for (int k = 0; k < Q; ++k) {
-                const float u0 = uc[k], v0 = vc[k], w0 = wc[k];
-                ou[k] = u0 + ((u0 - pu[k]) + su[k]);
-                ov[k] = v0 + ((v0 - pv[k]) + sv[k]);
-                ow[k] = w0 + ((w0 - pw[k]) + sw[k]);
-            }
+            const float4 pu4 = *reinterpret_cast<const float4*>(&st.pts[0][txt][tzt * Q]);
+            const float4 pv4 = *reinterpret_cast<const float4*>(&st.pts[1][txt][tzt * Q]);
+            const float4 pw4 = *reinterpret_cast<const float4*>(&st.pts[2][txt][tzt * Q]);
+            const float4 uc4 = *reinterpret_cast<const float4*>(&st.halo[0][c][r0]);
+            const float4 vc4 = *reinterpret_cast<const float4*>(&st.halo[1][c][r0]);
+            const float4 wc4 = *reinterpret_cast<const float4*>(&st.halo[2][c][r0]);
+            // nF = F + ((F - pF) + sF)
+            const float2 nu01 = padd(pr(uc4.x, uc4.y), padd(psub(pr(uc4.x, uc4.y), pr(pu4.x, pu4.y)), s2u[0]));
+            const float2 nu23 = padd(pr(uc4.z, uc4.w), padd(psub(pr(uc4.z, uc4.w), pr(pu4.z, pu4.w)), s2u[1]));
+            const float2 nv01 = padd(pr(vc4.x, vc4.y), padd(psub(pr(vc4.x, vc4.y), pr(pv4.x, pv4.y)), s2v[0]));
+            const float2 nv23 = padd(pr(vc4.z, vc4.w), padd(psub(pr(vc4.z, vc4.w), pr(pv4.z, pv4.w)), s2v[1]));
+            const float2 nw01 = padd(pr(wc4.x, wc4.y), padd(psub(pr(wc4.x, wc4.y), pr(pw4.x, pw4.y)), s2w[0]));
+            const float2 nw23 = padd(pr(wc4.z, wc4.w), padd(psub(pr(wc4.z, wc4.w), pr(pw4.z, pw4.w)), s2w[1]));
+            float ou[Q] = {nu01.x, nu01.y, nu23.x, nu23.y};
+            float ov[Q] = {nv01.x, nv01.y, nv23.x, nv23.y};
+            float ow[Q] = {nw01.x, nw01.y, nw23.x, nw23.y};
+            const float su[Q] = {s2u[0].x, s2u[0].y, s2u[1].x, s2u[1].y};
+            const float pu[Q] = {pu4.x, pu4.y, pu4.z, pu4.w};
+            const float uc[Q] = {uc4.x, uc4.y, uc4.z, uc4.w};
             if (mode == MODE_FWD) {
                 if (snap_step) {
 #pragma unroll
