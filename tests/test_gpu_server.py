@@ -162,3 +162,27 @@ def test_invalid_jobs_fail_at_submission():
         with pytest.raises(mnad.MnadError) as e:
             srv.submit(j)
         assert e.value.code == mnad._lib.E_ARG
+
+
+def test_tick_graphs_and_direct_launches_agree():
+    jobs_g, jobs_d = _mix(), _mix()
+    for jobs, graphs in ((jobs_g, True), (jobs_d, False)):
+        with mnad.Server(0, chunk_steps=32, graphs=graphs) as srv:
+            for t in [srv.submit(j) for j in jobs]:
+                srv.wait(t, timeout_s=300)
+    for a, b in zip(jobs_g, jobs_d):
+        _same(a, b)
+
+
+def test_fp16_snapshots_served_equal_a_plan_run():
+    """FP16 snapshot encodes are per-step host work, so these ticks launch
+    step by step; the outputs still equal mnad_run_jobs with the same codec."""
+    jobs = [j for j in _mix() if j.kind == "rtm"]
+    ref = [_copy(j) for j in jobs]
+    with mnad.Context(0, snapshot_codec="f16") as ctx:
+        ctx.run_jobs(ref)
+    with mnad.Server(0, chunk_steps=16, snapshot_codec="f16") as srv:
+        for t in [srv.submit(j) for j in jobs]:
+            srv.wait(t, timeout_s=300)
+    for a, b in zip(jobs, ref):
+        _same(a, b)
