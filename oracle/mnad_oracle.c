@@ -16,8 +16,10 @@
  *   - the forward loop of SRC/MNAD/fwd_PDE_exact_MNAD.m:92-157 and the
  *     adjoint loop of SRC/migration/Born_adj_MNAD.m:85-138 (with U_r read as
  *     U, Born_adj_MNAD.m:105-106).
- * PARITY UNPINNED against MATLAB itself (no MATLAB/Octave available, no
- * golden vectors in the reference); pinned against the sparse restatement.
+ * Pinned to the reference: it reproduces, to 1e-12, the outputs of the
+ * reference's own .m sources run under the MATLAB-subset interpreter
+ * oracle/mlite.py (fixtures tests/golden/golden_ref_*.npz; no MATLAB or
+ * Octave is available).
  *
  * Layout: column-major, z fastest: F[j + i*nz], j in [0,nz), i in [0,nx).
  * Indices passed in are 1-based, like the MATLAB call signature.

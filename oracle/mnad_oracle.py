@@ -24,11 +24,13 @@ for step, with these documented decisions:
   adjoint pairs column ``ncols-ttt+1`` (``Born_adj_MNAD.m:128``).  Columns past
   ``k`` are zero.  ``pairing="aligned"`` pairs column ``k-ttt+1`` instead.
 
-PARITY UNPINNED: the reference is MATLAB, neither MATLAB nor GNU Octave is
-available, and the reference ships no golden vectors or tests.  This
-restatement is cross-checked against an independent matrix-free FP64 C
-restatement (``oracle/mnad_oracle.c``) to ~1e-13, and against the fixtures in
-``tests/golden/`` that ``tests/golden/make_golden.py`` generated from it.
+Pinning: the reference is MATLAB and ships no golden vectors or tests, and
+neither MATLAB nor GNU Octave is available.  Its own ``.m`` sources were run
+under the MATLAB-subset interpreter ``oracle/mlite.py``
+(``tests/golden/make_reference_golden.py``); this restatement reproduces those
+runs (``tests/golden/golden_ref_*.npz``) to 1e-12 (``tests/test_reference_golden.py``).
+It is also cross-checked against the independent matrix-free FP64 C
+restatement (``oracle/mnad_oracle.c``) to ~1e-13.
 
 Indexing: arrays have MATLAB shape ``(nz, nx)`` (z = row, x = column) and
 are flattened column-major (``order="F"``), matching ``idx(j,i)=j+(i-1)*nz``

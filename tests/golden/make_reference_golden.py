@@ -1,0 +1,112 @@
+"""Golden fixtures produced by the reference's own MATLAB sources.
+
+Runs SRC/MNAD/*.m and SRC/migration/Born_adj_MNAD.m of the reference
+checkout (path in MNAD_REFERENCE, default /root/reference) under the MATLAB-
+subset interpreter oracle/mlite.py -- neither MATLAB nor Octave exists here --
+and stores their outputs:
+
+* golden_ref_rtm.npz: one RTM shot on a 40 x 52 layered model (true-model
+  forward, background forward with indx = 1 -> UU and illum, adjoint of the
+  scattered data -> Im) at three record lengths: nt = 240, where
+  floor(nt/T) < 2nf+1 (the reference's pairing shifted by one snapshot),
+  nt = 247 (aligned) and nt = 239, where floor(nt/T) > 2nf+1 and UU grows
+  past its preallocated columns;
+* golden_ref_config1.npz: config 1 (201 x 201, 20-point CPML, 2000 m/s,
+  20 Hz Ricker at the centre, 201 receivers on row 21, nt = 1000), the
+  reference's own CPU case.
+
+The only change applied to the reference sources is the one-token fix of
+Born_adj_MNAD.m:105-106 (undefined U_r read as U); the adjoint receives the
+data as a cell {data}, as Born_adj_MNAD.m:50 expects.  The Ricker wavelet of
+the drivers (main_Acoustic_RTM.m:138-140) is an input, computed here.
+
+Usage: python tests/golden/make_reference_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "mnad-modeling-rtm_gb300"))
+
+from oracle import mlite  # noqa: E402
+
+REF = os.environ.get("MNAD_REFERENCE", "/root/reference")
+NAMES = ["Auu", "Auv", "Auw", "Avu", "Avv", "Avw", "Awu", "Awv", "Aww"]
+
+
+def S(x):
+    return np.array([[float(x)]])
+
+
+def ricker(fc, dt, nt):
+    t = np.arange(nt) * dt
+    tau = np.pi * (t - 1.1 / fc) * fc
+    return ((1 - 2 * tau ** 2) * np.exp(-tau ** 2)).reshape(-1, 1)
+
+
+def interpreter():
+    return mlite.Interpreter([os.path.join(REF, "SRC", "MNAD"), os.path.join(REF, "SRC", "migration")],
+                             patches={"Born_adj_MNAD": [("U_r(:)", "U(:)")]})
+
+
+def operators(it, dx, dz, dt, v):
+    return [it.call(n + "_gen", [S(dx), S(dz), S(dt), v])[0] for n in NAMES]
+
+
+def rtm_case(it, nt, seed=0):
+    nz, nx, d = 40, 52, 8
+    dx = dz = 10.0
+    dt = 1e-3
+    z = np.arange(nz)[:, None] * np.ones((1, nx))
+    x = np.ones((nz, 1)) * np.arange(nx)[None, :]
+    v = 1700.0 + 600.0 * (z >= 20) + 500.0 * (z >= 30)
+    v = v + 250.0 * np.exp(-((z - 25) ** 2 + (x - 30) ** 2) / (2 * 4.0 ** 2))
+    vs = 1700.0 + 1100.0 * (z / (nz - 1)) + 0.0 * x          # smooth background
+    w = ricker(25.0, dt, nt)
+    xr = np.arange(d + 1, nx - d + 1, dtype=float).reshape(1, -1)
+    zr = np.full(xr.shape, d + 2.0)
+    zs, xs, ss = d + 2, 27, 5
+    A = operators(it, dx, dz, dt, v)
+    As = operators(it, dx, dz, dt, vs)
+    common = [S(dx), S(xs), xr, S(dz), S(zs), zr]
+    data = it.call("fwd_PDE_exact_MNAD", common + [v, S(dt), S(nt), w, S(d), S(ss)] + A + [S(0)])[0].items[0]
+    datas = it.call("fwd_PDE_exact_MNAD", common + [vs, S(dt), S(nt), w, S(d), S(ss)] + As + [S(1)])[0].items[0]
+    UU = it.files[f"./Wavefields/UU_{ss}"]["UU"]
+    illum = it.files[f"./Illuminations/illum_{ss}"]["illum"]
+    res = data - datas
+    Im = it.call("Born_adj_MNAD", [S(dx), S(dz), S(nt), S(dt), vs, xr, zr, mlite.Cell([res]), S(d), S(ss)] + As)[0]
+    return dict(v=v, vs=vs, dx=dx, dz=dz, dt=dt, nt=nt, d=d, w=w.ravel(), xr=xr.ravel(), zr=zr.ravel(), zs=zs,
+                xs=xs, data=data, datas=datas, UU=UU, illum=illum, Im=Im.ravel())
+
+
+def config1_case(it):
+    nz = nx = 201
+    d, nt, dt, dx = 20, 1000, 1e-3, 10.0
+    v = np.full((nz, nx), 2000.0)
+    w = ricker(20.0, dt, nt)
+    xr = np.arange(1, nx + 1, dtype=float).reshape(1, -1)
+    zr = np.full(xr.shape, 21.0)
+    A = operators(it, dx, dx, dt, v)
+    data = it.call("fwd_PDE_exact_MNAD", [S(dx), S(101), xr, S(dx), S(101), zr, v, S(dt), S(nt), w, S(d), S(1)] +
+                   A + [S(0)])[0].items[0]
+    return dict(dx=dx, dt=dt, nt=nt, d=d, v0=2000.0, nz=nz, nx=nx, zs=101, xs=101, zr=21, fc=20.0, data=data)
+
+
+def main():
+    it = interpreter()
+    cases = {"a": rtm_case(it, 240), "b": rtm_case(it, 247), "c": rtm_case(it, 239)}
+    out = {f"{n}_{k}": val for n, case in cases.items() for k, val in case.items()}
+    np.savez_compressed(os.path.join(HERE, "golden_ref_rtm.npz"), **out)
+    c = config1_case(it)
+    np.savez_compressed(os.path.join(HERE, "golden_ref_config1.npz"), **c)
+    for name, case in cases.items():
+        print(name, "nt", case["nt"], "UU", case["UU"].shape, "|Im|", np.linalg.norm(case["Im"]))
+    print("config1 |data|", np.linalg.norm(c["data"]))
+
+
+if __name__ == "__main__":
+    main()
