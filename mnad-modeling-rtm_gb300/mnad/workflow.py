@@ -10,6 +10,7 @@ wavelet is ``(1-2 tau^2) exp(-tau^2)``, ``tau = pi (t - 1.1/fc) fc``
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 from typing import List, Optional
 
@@ -294,3 +295,101 @@ def served_shot_job(sj: ServedJob, pools, d_pml: int = 20):
     return ShotJob(kind=sj.kind, v=v, vs=vs if sj.kind == "rtm" else None, dx=10.0, dz=10.0, dt=1e-3, nt=sj.nt,
                    d_pml=d_pml, zs=float(d_pml + 2), xs=float(sj.xs), zr=zr, xr=xr, w=ricker(sj.fc, 1e-3, sj.nt),
                    keep_data=True)
+
+
+# ---------------------------------------------------------------------------
+# Acquisition geometry and model smoothing of the reference's drivers
+
+def acquisi(V, dx, dz, zsc, zrc, h_offset, ds, dr, slag, rlag, acq_type: str = "fixspread", manual=None):
+    """Source and receiver positions in metres, as ``SRC/MNAD/acquisi.m``.
+
+    ``V`` is the unpadded model (nz x nx); ``zsc`` / ``zrc`` source and
+    receiver depths, ``h_offset`` the half offset, ``ds`` / ``dr`` the source
+    and receiver spacings, ``slag`` / ``rlag`` the edge margins (metres).
+    ``acq_type``: 'fixspread', 'onesided', 'splitspread', 'obn' (sources on
+    the sea floor below a constant-velocity water column, receivers at
+    ``zsc``) or 'arbitrary' (``manual`` = dict of grid indices xs, zs, xr,
+    zr).  Returns ``(Source, Receiver)``: Source is 2 x ns (x; z), Receiver
+    a list of ns (x_metres, z_metres) pairs.  Grid indices are 1-based and
+    unpadded; the drivers add d_pml (``padded_indices``)."""
+    V = np.asarray(V, dtype=np.float64)
+    nz, nx = V.shape
+    ds = int(np.trunc(ds / dx)) or 1
+    dr = int(np.trunc(dr / dx)) or 1
+    kind = acq_type.lower()
+
+    def rng(a, step, b):
+        return np.arange(a, b + 1, step, dtype=np.float64) if b >= a else np.zeros(0)
+
+    if kind == "arbitrary":
+        if manual is None:
+            raise ValueError("acqType is 'arbitrary' but manualGeom was not provided")
+        for key in ("xs", "zs", "xr", "zr"):
+            if key not in manual:
+                raise ValueError(f"manualGeom is missing required field '{key}'")
+        xs = np.asarray(manual["xs"], dtype=np.float64).ravel()
+        zs = np.asarray(manual["zs"], dtype=np.float64).ravel()
+        xr = [np.asarray(x, dtype=np.float64).ravel() for x in manual["xr"]]
+        zr = [np.asarray(z, dtype=np.float64).ravel() for z in manual["zr"]]
+    else:
+        xs = rng(math.ceil(slag / dx), ds, nx - math.floor(slag / dx))
+        zs = np.zeros_like(xs) + math.floor(zsc / dz)
+        h_off = math.floor(h_offset / dx)
+        last = nx - math.floor(rlag / dx)
+        xr, zr = [], []
+        if kind == "obn":
+            water = V[0, 0]
+            xs = rng(math.ceil(rlag / dx), dr, last)
+            zs = np.array([float(np.flatnonzero(V[:, int(x) - 1] == water).max() + 1) for x in xs])
+            for _ in xs:
+                r = rng(math.ceil(slag / dx), ds, nx - math.floor(slag / dx))
+                xr.append(r)
+                zr.append(0.0 * r + math.floor(zsc / dz))
+        else:
+            for s in xs:
+                if kind == "onesided":
+                    r = rng(s, dr, last) if s + h_off > last else rng(s, dr, s + h_off - 1)
+                elif kind == "splitspread":
+                    if s + h_off > last:
+                        r = rng(s - h_off, dr, last)
+                    elif s - h_off <= 0:
+                        r = rng(1, dr, s + h_off - 1)
+                    else:
+                        r = rng(s - h_off, dr, s + h_off - 1)
+                elif kind == "fixspread":
+                    r = rng(math.ceil(rlag / dx), dr, last)
+                else:
+                    raise ValueError(f"unknown acqType {acq_type!r}; use 'splitspread', 'onesided', 'obn', "
+                                     "'fixspread' or 'arbitrary'")
+                xr.append(r)
+                zr.append(0.0 * r + math.floor(zrc / dz))
+    Source = np.vstack([dx * xs, dz * zs])
+    Receiver = [(dx * x, dz * z) for x, z in zip(xr, zr)]
+    return Source, Receiver
+
+
+def padded_indices(Source, Receiver, dx, dz, d_pml):
+    """1-based padded grid indices of the drivers (``main_Acoustic_RTM.m:124-130``):
+    index = d_pml + metres / spacing.  Returns (xs, zs, [xr], [zr])."""
+    xs = d_pml + np.asarray(Source[0]) / dx
+    zs = d_pml + np.asarray(Source[1]) / dz
+    return xs, zs, [d_pml + x / dx for x, _ in Receiver], [d_pml + z / dz for _, z in Receiver]
+
+
+def v_smooth(v, s1: int, s2: int, nit: int) -> np.ndarray:
+    """Smoothed migration model of ``SRC/MNAD/v_smooth.m``: ``nit`` passes of
+    an s1 x s2 box average of the slowness with edge replication."""
+    s0 = 1.0 / np.asarray(v, dtype=np.float64)
+    h1, h2 = (s1 - 1) // 2, (s2 - 1) // 2
+    n1, n2 = s0.shape
+    for _ in range(nit):
+        p = np.pad(s0, ((h1, h1), (h2, h2)), mode="edge")
+        # window sums: columns first, then rows, as sum(sum(window))
+        cz = np.zeros((p.shape[0] - 2 * h1, p.shape[1]))
+        for a in range(s1):
+            cz += p[a:a + n1, :]
+        acc = np.zeros((n1, n2))
+        for b in range(s2):
+            acc += cz[:, b:b + n2]
+        s0 = acc / (s1 * s2)
+    return 1.0 / s0

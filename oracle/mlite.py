@@ -35,8 +35,23 @@ import scipy.sparse as sp
 
 
 class Cell:
-    def __init__(self, items=None):
+    """A cell array: items in column-major order, shape (rows, cols)."""
+
+    def __init__(self, items=None, shape=None):
         self.items = list(items or [])
+        self.shape = shape or (1, len(self.items))
+
+
+class MatlabError(RuntimeError):
+    def __init__(self, ident, msg):
+        self.identifier = ident
+        super().__init__(f"{ident}: {msg}")
+
+
+def _case_match(subject, option):
+    if isinstance(subject, str) or isinstance(option, str):
+        return isinstance(subject, str) and isinstance(option, str) and subject == option
+    return bool(np.all(num(subject) == num(option)))
 
 
 def num(x):
@@ -74,12 +89,13 @@ TOKEN = re.compile(r"""
   | (?P<cont>\.\.\.[^\n]*\n)
   | (?P<comment>%[^\n]*)
   | (?P<nl>\n)
-  | (?P<num>(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?)
+  | (?P<num>(?:\d+(?:\.(?![*/^'\\])\d*)?|\.\d+)(?:[eE][+-]?\d+)?)
   | (?P<id>[A-Za-z_]\w*)
   | (?P<op>\.\^|\.\*|\./|\.'|==|~=|<=|>=|&&|\|\||[-+*/^\\<>&|~=(){}\[\],;:'@.])
 """, re.VERBOSE)
 
-KEYWORDS = {"function", "end", "for", "if", "elseif", "else", "while", "return", "break", "continue"}
+KEYWORDS = {"function", "end", "for", "if", "elseif", "else", "while", "return", "break", "continue", "switch",
+            "case", "otherwise"}
 
 
 def lex(src):
@@ -116,8 +132,9 @@ def lex(src):
         if kind in ("comment", "cont"):
             continue
         if kind == "ws":
-            # inside [] or {} whitespace may separate elements: mark it
-            if depth and depth[-1] in "[{" and toks:
+            # whitespace after a token: separates elements inside [] / {} and
+            # marks command syntax ("clear a b") at statement level
+            if toks:
                 toks[-1] = (toks[-1][0], toks[-1][1], True)
             continue
         if kind == "op":
@@ -249,6 +266,21 @@ class Parser:
                         self.expect("end")
                         break
                 return ("if", arms, other)
+            if k == "switch":
+                self.next()
+                subject = self.expr()
+                cases, other = [], []
+                self.skip_sep()
+                while True:
+                    if self.accept("case"):
+                        label = self.expr()
+                        cases.append((label, self.block(("case", "otherwise", "end"))))
+                    elif self.accept("otherwise"):
+                        other = self.block(("case", "otherwise", "end"))
+                    else:
+                        self.expect("end")
+                        break
+                return ("switch", subject, cases, other)
             if k in ("return", "break", "continue"):
                 self.next()
                 return (k,)
@@ -275,6 +307,13 @@ class Parser:
                     targets.append(self.postfix())
                 self.expect("=")
                 return ("massign", targets, self.expr())
+        # command syntax: name word word ... (e.g. "clear xz zs", "save Source Source")
+        if tok[0] == "id" and tok[2] and self.peek(1)[0] in ("id", "num") and self.peek(2)[1] not in ("=", "("):
+            name = self.next()[1]
+            words = []
+            while self.peek()[0] in ("id", "num", "kw") and self.peek()[1] not in ("end",):
+                words.append(("str", self.next()[1]))
+            return ("expr", ("index", ("id", name), words))
         # assignment or expression statement
         start = self.i
         if tok[0] == "id":
@@ -390,6 +429,9 @@ class Parser:
             elif tok[1] in ("'", ".'") and tok[0] == "op":
                 self.next()
                 a = ("transpose", a)
+            elif tok[1] == "." and tok[0] == "op" and self.peek(1)[0] == "id":
+                self.next()
+                a = ("field", a, self.next()[1])
             else:
                 return a
 
@@ -568,6 +610,15 @@ class Interpreter:
                     self.block(body, env)
                     return
             self.block(s[2], env)
+        elif k == "switch":
+            subject = self.value(s[1], env)
+            for label, body in s[2]:
+                lv = self.value(label, env)
+                options = lv.items if isinstance(lv, Cell) else [lv]
+                if any(_case_match(subject, o) for o in options):
+                    self.block(body, env)
+                    return
+            self.block(s[3], env)
         elif k == "return":
             raise Return()
         elif k == "break":
@@ -638,6 +689,8 @@ class Interpreter:
             while len(cell.items) <= k:
                 cell.items.append(np.zeros((0, 0)))
             cell.items[k] = val
+            if cell.shape[0] <= 1:
+                cell.shape = (1, len(cell.items))
             env[name] = cell
             return
         if target[0] != "index" or target[1][0] != "id":
@@ -712,10 +765,13 @@ class Interpreter:
             return out
         if k == "cindex":
             c = self.value(e[1], env)
-            kidx = int(scalar(self.value(e[2][0], env))) - 1
             if not isinstance(c, Cell):
                 raise TypeError("brace indexing of a non-cell")
+            sub = [int(scalar(self.value(a, env))) - 1 for a in e[2]]
+            kidx = sub[0] if len(sub) == 1 else sub[0] + sub[1] * c.shape[0]
             return c.items[kidx]
+        if k == "field":
+            return self.value(e[1], env)[e[2]]
         if k == "transpose":
             v = self.value(e[1], env)
             return v.T.copy() if not isinstance(v, str) else num(v).T
@@ -738,6 +794,15 @@ class Interpreter:
         if k == "bin":
             return binop(e[1], self.value(e[2], env), self.value(e[3], env))
         if k == "matrix":
+            if not e[1]:
+                return np.zeros((0, 0))
+            cells = [[self.value(x, env) for x in r] for r in e[1]]
+            if any(isinstance(v, Cell) for r in cells for v in r):
+                # concatenation of cell rows of equal width: [a ; b] -> 2 x n cell
+                rows_ = [sum((v.items for v in r), []) for r in cells]
+                ncol = len(rows_[0])
+                items = [rows_[i][j] for j in range(ncol) for i in range(len(rows_))]
+                return Cell(items, (len(rows_), ncol))
             rows = []
             for r in e[1]:
                 vals = [self.value(x, env) for x in r]
@@ -748,7 +813,8 @@ class Interpreter:
                 rows.append(np.hstack(parts) if parts else np.zeros((0, 0)))
             if len(rows) == 1:
                 return rows[0]
-            return np.vstack([num(r) for r in rows if num(r).size])
+            parts = [num(r) for r in rows if num(r).size]
+            return np.vstack(parts) if parts else np.zeros((0, 0))
         if k == "cell":
             return Cell([self.value(x, env) for r in e[1] for x in r])
         raise SyntaxError(f"expression {k}")
@@ -837,6 +903,8 @@ def _size(it, a, nout):
 
 
 def _zeros(it, a, nout):
+    if len(a) == 1 and num(a[0]).size == 2:
+        a = [num(a[0]).flat[0], num(a[0]).flat[1]]
     dims = [int(scalar(x)) for x in a] or [1]
     if len(dims) == 1:
         dims = dims * 2
@@ -923,6 +991,17 @@ BUILTINS = {
     "tic": lambda it, a, n: [],
     "toc": lambda it, a, n: [np.array([[0.0]])],
     "pi": lambda it, a, n: [np.array([[math.pi]])],
+    "fix": lambda it, a, n: [np.trunc(num(a[0]))],
+    "lower": lambda it, a, n: [a[0].lower()],
+    "cell": lambda it, a, n: [Cell([np.zeros((0, 0))] * (int(scalar(a[0])) * int(scalar(a[1]))),
+                                   (int(scalar(a[0])), int(scalar(a[1]))))],
+    "sum": lambda it, a, n: [np.sum(num(a[0]), axis=0, keepdims=True) if num(a[0]).shape[0] > 1
+                             else np.sum(num(a[0]), axis=1, keepdims=True)],
+    "find": lambda it, a, n: [(np.flatnonzero(num(a[0]).ravel(order="F")) + 1.0).reshape(-1, 1)],
+    "datetime": lambda it, a, n: ["now"],
+    "string": lambda it, a, n: [str(a[0])],
+    "isfield": lambda it, a, n: [np.array([[isinstance(a[0], dict) and a[1] in a[0]]])],
+    "error": lambda it, a, n: (_ for _ in ()).throw(MatlabError(a[0], a[1] if len(a) > 1 else "")),
 }
 
 
@@ -943,7 +1022,11 @@ def _install_saveload():
             raise NotImplementedError("load into a struct")
         env.update({k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in data.items()})
         return []
-    return {"save": save, "load": load}
+    def clear(it, a, nout, env=None):
+        for name in a:
+            env.pop(name, None)
+        return []
+    return {"save": save, "load": load, "clear": clear}
 
 
 ENV_BUILTINS = _install_saveload()

@@ -13,7 +13,10 @@ and stores their outputs:
   past its preallocated columns;
 * golden_ref_config1.npz: config 1 (201 x 201, 20-point CPML, 2000 m/s,
   20 Hz Ricker at the centre, 201 receivers on row 21, nt = 1000), the
-  reference's own CPU case.
+  reference's own CPU case;
+* golden_ref_prep.npz: SRC/MNAD/acquisi.m for the 'fixspread', 'onesided',
+  'splitspread' and 'obn' geometries and SRC/MNAD/v_smooth.m on a random
+  model (the drivers' acquisition and migration-model preparation).
 
 The only change applied to the reference sources is the one-token fix of
 Born_adj_MNAD.m:105-106 (undefined U_r read as U); the adjoint receives the
@@ -96,11 +99,39 @@ def config1_case(it):
     return dict(dx=dx, dt=dt, nt=nt, d=d, v0=2000.0, nz=nz, nx=nx, zs=101, xs=101, zr=21, fc=20.0, data=data)
 
 
+ACQ = dict(dx=10.0, dz=10.0, zsc=20.0, zrc=20.0, h_offset=500.0, ds=100.0, dr=20.0, slag=50.0, rlag=30.0)
+
+
+def prep_case(it):
+    rng = np.random.default_rng(3)
+    V = np.full((60, 200), 2400.0)
+    V[:7, :] = 1500.0                                  # water column for the 'obn' geometry
+    V[7:, 80:] += 300.0
+    out = dict(V=V, **{f"acq_{k}": v for k, v in ACQ.items()})
+    a = ACQ
+    for kind in ("fixspread", "onesided", "splitspread", "obn"):
+        Src, Rec = it.call("acquisi", [V, S(a["dx"]), S(a["dz"]), S(a["zsc"]), S(a["zrc"]), S(a["h_offset"]),
+                                       S(a["ds"]), S(a["dr"]), S(a["slag"]), S(a["rlag"]), kind,
+                                       np.zeros((1, 1)) == 1], 2)
+        ns = Src.shape[1]
+        xr = [Rec.items[2 * k].ravel() for k in range(ns)]
+        zr = [Rec.items[2 * k + 1].ravel() for k in range(ns)]
+        out[f"{kind}_Source"] = Src
+        out[f"{kind}_xr"] = np.concatenate(xr)
+        out[f"{kind}_zr"] = np.concatenate(zr)
+        out[f"{kind}_nr"] = np.array([len(x) for x in xr])
+    vm = rng.uniform(1500.0, 3500.0, (24, 30))
+    out["vsm_in"] = vm
+    out["vsm_out"] = it.call("v_smooth", [vm, S(5), S(3), S(2)])[0]
+    return out
+
+
 def main():
     it = interpreter()
     cases = {"a": rtm_case(it, 240), "b": rtm_case(it, 247), "c": rtm_case(it, 239)}
     out = {f"{n}_{k}": val for n, case in cases.items() for k, val in case.items()}
     np.savez_compressed(os.path.join(HERE, "golden_ref_rtm.npz"), **out)
+    np.savez_compressed(os.path.join(HERE, "golden_ref_prep.npz"), **prep_case(it))
     c = config1_case(it)
     np.savez_compressed(os.path.join(HERE, "golden_ref_config1.npz"), **c)
     for name, case in cases.items():

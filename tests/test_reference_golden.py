@@ -116,3 +116,24 @@ def test_growth_sparse_cells_and_power_precedence():
     assert np.array_equal(b.ravel(), np.array([1, 32]))
     assert c[0, 0] == 4.0
     assert bool(d[0, 0])
+
+
+# ---- acquisition geometry and model smoothing (the drivers' preparation) -----
+
+@pytest.mark.parametrize("kind", ["fixspread", "onesided", "splitspread", "obn"])
+def test_acquisition_matches_the_reference(kind):
+    from mnad import workflow
+    g = np.load(os.path.join(GOLDEN, "golden_ref_prep.npz"))
+    a = {k[4:]: float(g[k]) for k in g.files if k.startswith("acq_")}
+    Source, Receiver = workflow.acquisi(g["V"], a["dx"], a["dz"], a["zsc"], a["zrc"], a["h_offset"], a["ds"],
+                                        a["dr"], a["slag"], a["rlag"], kind)
+    assert np.array_equal(Source, g[f"{kind}_Source"])
+    assert [len(x) for x, _ in Receiver] == list(g[f"{kind}_nr"])
+    assert np.array_equal(np.concatenate([x for x, _ in Receiver]), g[f"{kind}_xr"])
+    assert np.array_equal(np.concatenate([z for _, z in Receiver]), g[f"{kind}_zr"])
+
+
+def test_v_smooth_matches_the_reference():
+    from mnad import workflow
+    g = np.load(os.path.join(GOLDEN, "golden_ref_prep.npz"))
+    assert rel(workflow.v_smooth(g["vsm_in"], 5, 3, 2), g["vsm_out"]) <= TOL
