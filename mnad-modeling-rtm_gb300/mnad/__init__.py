@@ -10,5 +10,6 @@
 from ._lib import MnadError, lib  # noqa: F401
 from .api import Context, Plan, Server, ShotJob  # noqa: F401
 from .reference_api import Born_adj_MNAD, fwd_PDE_exact_MNAD  # noqa: F401
+from . import drivers  # noqa: F401,E402
 
 __all__ = ["Context", "Plan", "Server", "ShotJob", "MnadError", "fwd_PDE_exact_MNAD", "Born_adj_MNAD", "lib"]

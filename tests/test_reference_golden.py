@@ -137,3 +137,16 @@ def test_v_smooth_matches_the_reference():
     from mnad import workflow
     g = np.load(os.path.join(GOLDEN, "golden_ref_prep.npz"))
     assert rel(workflow.v_smooth(g["vsm_in"], 5, 3, 2), g["vsm_out"]) <= TOL
+
+
+def test_driver_grid_and_time_rules():
+    """main_Acoustic_RTM.m:70-90 on its own example model (1500 / 2500 m/s,
+    fc = 15 Hz, 3 s): dx = floor(1500 / 112.5) = 13, dt = 0.8 * 0.65 *
+    13.33 / 2500, nt = length(0:dt:3-dt)."""
+    from mnad import drivers
+    V = np.full((100, 200), 1500.0)
+    V[69:, :] = 2500.0
+    dx, dz, dt, nt = drivers.grid_and_time(V, 15.0, 3.0)
+    assert (dx, dz) == (13.0, 13.0)
+    assert dt == 0.8 * ((0.65 * (1500.0 / (2.5 * 45.0))) / 2500.0)
+    assert nt == len(mlite.colon(0.0, dt, 3.0 - dt).ravel())
