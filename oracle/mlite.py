@@ -580,7 +580,9 @@ class Interpreter:
                     self.assign(t, v, env)
         elif k == "expr":
             e = s[1]
-            if e[0] == "id" and e[1] not in env:
+            if e[0] == "index" and e[1][0] == "id" and e[1][1] in ENV_BUILTINS and e[1][1] not in env:
+                ENV_BUILTINS[e[1][1]](self, [self.value(x, env) for x in e[2]], 0, env=env)
+            elif e[0] == "id" and e[1] not in env:
                 self.call(e[1], [], 0)
             elif e[0] == "index" and e[1][0] == "id" and e[1][1] not in env:
                 self.call(e[1][1], [self.value(a, env) for a in e[2]], 0)
@@ -955,11 +957,6 @@ def _norm_name(name):
     return name[:-4] if name.endswith(".mat") else name
 
 
-def _save(it, a, nout):
-    # called with the caller's variables: the evaluator passes them by name
-    raise RuntimeError("save is handled by the interpreter")
-
-
 BUILTINS = {
     "size": _size,
     "zeros": _zeros,
@@ -1005,11 +1002,9 @@ BUILTINS = {
 }
 
 
-class _SaveLoad:
-    """save(name, 'var', ...) / load(name) against the interpreter's store."""
-
-
 def _install_saveload():
+    """save(name, 'var', ...) / load(name) / clear(names) work on the caller's
+    variables: the interpreter passes them the caller's environment."""
     def save(it, a, nout, env=None):
         name = _norm_name(a[0])
         it.files[name] = {v: env[v].copy() if isinstance(env[v], np.ndarray) else env[v] for v in a[1:]}
@@ -1030,17 +1025,3 @@ def _install_saveload():
 
 
 ENV_BUILTINS = _install_saveload()
-
-_orig_stmt = Interpreter.stmt
-
-
-def _stmt_with_env_builtins(self, s, env):
-    if s[0] == "expr" and s[1][0] == "index" and s[1][1][0] == "id" and s[1][1][1] in ENV_BUILTINS \
-            and s[1][1][1] not in env:
-        args = [self.value(x, env) for x in s[1][2]]
-        ENV_BUILTINS[s[1][1][1]](self, args, 0, env=env)
-        return
-    _orig_stmt(self, s, env)
-
-
-Interpreter.stmt = _stmt_with_env_builtins
