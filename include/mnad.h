@@ -62,7 +62,9 @@ enum { MNAD_SNAP_F32 = 0, MNAD_SNAP_BF16 = 1, MNAD_SNAP_F16 = 2 };
  * ALIGNED:   column k-ttt+1 (source and receiver fields at the same time). */
 enum { MNAD_PAIR_REFERENCE = 0, MNAD_PAIR_ALIGNED = 1 };
 
-/* Step kernel choice. */
+/* Step kernel choice.  AUTO picks per launch group (propagations of one grid
+ * size advancing together): the one-thread-per-point kernel below a million
+ * point-updates per launch, the persistent TMA kernel above. */
 enum { MNAD_KERNEL_AUTO = 0, MNAD_KERNEL_DIRECT = 1, MNAD_KERNEL_TMA = 2 };
 
 typedef struct mnad_options {

@@ -72,7 +72,7 @@ struct __align__(16) PropDesc {
     int tile_base;     // first global tile of this propagation
     int s_off;         // global step at which this propagation started (even)
     int s_begin, s_end;  // global steps [s_begin, s_end) in which it may advance
-    int ntz, ntx;      // tiles along z / x
+    int ntz, ntx;      // receiver-bucket (TMA_TZ x TMA_TX) tiles along z / x
     float* fld[2][3];  // [time level][U,V,W], storage origin (halo included)
     const float* r;    // v^2 dt^2, same storage
     float* mx;         // x-strip memory variables [side 2][var 9][d][ld]
@@ -84,15 +84,15 @@ struct __align__(16) PropDesc {
     // r_src*w(tt) injected at each step (fwd_PDE_exact_MNAD.m:111)
     int src;                 // -1: none
     const float* src_amp;    // [nt]
-    // receivers, bucketed per tile: entries tile_rec[t]..tile_rec[t+1]
+    // receivers, bucketed per TMA_TZ x TMA_TX tile (for every step kernel):
+    // entries tile_rec[t]..tile_rec[t+1]
     int nr;
     const int* rec_pt;       // storage offset of each entry
     const int* rec_id;       // receiver column rr of each entry
     const double* rec_r;     // r at the receiver (adjoint injection scale)
     const int* tile_rec;     // [ntz*ntx + 1]
-    const int* col_rec;      // [ntz*ntx*TX + 1]: entries of local column c of tile t
-                             // are col_rec[t*TX + c] .. col_rec[t*TX + c+1] (TX: the
-                             // tile width of the kernel the propagation was built for)
+    const int* col_rec;      // [ntz*ntx*TMA_TX + 1]: entries of local column c of tile t
+                             // are col_rec[t*TMA_TX + c] .. col_rec[t*TMA_TX + c+1]
     double* data;            // [nr][nt] (column-major nt x nr): fwd out / adj in
     double* datav;           // optional fwd outputs
     double* dataw;

@@ -118,8 +118,31 @@ void download(Context& ctx, void* dst, const void* src, size_t bytes)
 // ---------------------------------------------------------------------------
 TileCfg tile_cfg(int kernel)
 {
-    if (kernel == MNAD_KERNEL_DIRECT) return TileCfg{MNAD_KERNEL_DIRECT, DIRECT_TZ, DIRECT_TX};
-    return TileCfg{MNAD_KERNEL_TMA, TMA_TZ, TMA_TX};
+    return TileCfg{kernel, TMA_TZ, TMA_TX};
+}
+
+void bucket_receivers(int nz, int nx, int ld, const std::vector<int>& zr, const std::vector<int>& xr,
+                      const double* v, double dt, int mode, RecBuckets& out)
+{
+    const int ntz = (nz + TMA_TZ - 1) / TMA_TZ, ntx = (nx + TMA_TX - 1) / TMA_TX;
+    const int ntiles = ntz * ntx, nb = ntiles * TMA_TX, nr = (int)zr.size();
+    std::vector<int> cnt(nb + 1, 0);
+    auto bucket = [&](int k) { return ((zr[k] / TMA_TZ) + (xr[k] / TMA_TX) * ntz) * TMA_TX + xr[k] % TMA_TX; };
+    for (int k = 0; k < nr; ++k) cnt[1 + bucket(k)]++;
+    for (int b = 0; b < nb; ++b) cnt[b + 1] += cnt[b];
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    out.pt.assign(nr, 0);
+    out.id.assign(nr, 0);
+    out.rr.assign(nr, 0.0);
+    for (int k = 0; k < nr; ++k) {
+        const int e = fill[bucket(k)]++;
+        out.pt[e] = (int)((size_t)(xr[k] + HX) * ld + (zr[k] + HZ));
+        out.id[e] = k;
+        out.rr[e] = r_of(v[(size_t)zr[k] + (size_t)xr[k] * nz], dt, mode);
+    }
+    out.tile_rec.assign(ntiles + 1, 0);
+    for (int t = 0; t <= ntiles; ++t) out.tile_rec[t] = cnt[(size_t)t * TMA_TX];
+    out.col_rec = std::move(cnt);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
@@ -267,8 +290,9 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     D.s_begin = INT_MIN;
     D.s_end = INT_MAX;
     D.mode = s.mode; D.nt = s.nt; D.nz = nz; D.nx = nx; D.ld = ld; D.d = d; D.dpz = dpz; D.zb0 = zb0;
-    D.ntz = (nz + tc.tz - 1) / tc.tz;
-    D.ntx = (nx + tc.tx - 1) / tc.tx;
+    (void)tc;
+    D.ntz = (nz + TMA_TZ - 1) / TMA_TZ;      // receiver buckets use the TMA tiling for every kernel
+    D.ntx = (nx + TMA_TX - 1) / TMA_TX;
     for (int t = 0; t < 2; ++t)
         for (int f = 0; f < 3; ++f) D.fld[t][f] = fields.as<float>() + (size_t)(t * 3 + f) * S;
     D.r = r_ext ? r_ext : r.as<float>();
@@ -296,32 +320,20 @@ void Prop::build(Context& ctx, const TileCfg& tc)
         D.src_amp = src_amp.as<float>();
     }
 
-    // Receivers bucketed by tile and, within a tile, by column (stable
-    // counting sort): the entries of tile t are tile_rec[t] .. tile_rec[t+1],
-    // those of its local column c are col_rec[t*tx + c] .. col_rec[t*tx + c+1].
+    // Receivers bucketed by TMA tile and column (bucket_receivers).
     const int nr = (int)s.zr.size();
-    const int ntiles = D.ntz * D.ntx;
-    const int nb = ntiles * tc.tx;
-    std::vector<int> cnt(nb + 1, 0), pt(nr), id(nr);
-    std::vector<double> rr(nr);
-    auto bucket = [&](int k) { return ((s.zr[k] / tc.tz) + (s.xr[k] / tc.tx) * D.ntz) * tc.tx + s.xr[k] % tc.tx; };
-    for (int k = 0; k < nr; ++k) cnt[1 + bucket(k)]++;
-    for (int b = 0; b < nb; ++b) cnt[b + 1] += cnt[b];
-    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-    for (int k = 0; k < nr; ++k) {
-        const int e = fill[bucket(k)]++;
-        pt[e] = off(s.zr[k], s.xr[k]);
-        id[e] = k;
-        rr[e] = r_of(s.v[(size_t)s.zr[k] + (size_t)s.xr[k] * nz], s.dt, s.mode);
-    }
+    RecBuckets rb;
+    bucket_receivers(nz, nx, ld, s.zr, s.xr, s.v, s.dt, s.mode, rb);
+    const std::vector<int>& pt = rb.pt;
+    const std::vector<int>& id = rb.id;
+    const std::vector<double>& rr = rb.rr;
     D.nr = nr;
-    tile_rec_host.assign(ntiles + 1, 0);
-    for (int t = 0; t <= ntiles; ++t) tile_rec_host[t] = cnt[(size_t)t * tc.tx];
-    tile_rec = DevMem(&ctx, (ntiles + 1) * sizeof(int));
-    upload(ctx, tile_rec.get(), tile_rec_host.data(), (ntiles + 1) * sizeof(int));
+    tile_rec_host = rb.tile_rec;
+    tile_rec = DevMem(&ctx, tile_rec_host.size() * sizeof(int));
+    upload(ctx, tile_rec.get(), tile_rec_host.data(), tile_rec_host.size() * sizeof(int));
     D.tile_rec = tile_rec.as<int>();
-    col_rec = DevMem(&ctx, (size_t)(nb + 1) * sizeof(int));
-    upload(ctx, col_rec.get(), cnt.data(), (size_t)(nb + 1) * sizeof(int));
+    col_rec = DevMem(&ctx, rb.col_rec.size() * sizeof(int));
+    upload(ctx, col_rec.get(), rb.col_rec.data(), rb.col_rec.size() * sizeof(int));
     D.col_rec = col_rec.as<int>();
     if (nr > 0) {
         rec_pt = DevMem(&ctx, nr * sizeof(int));
@@ -557,6 +569,13 @@ void Batch::finalize()
         nsteps_ = std::max(nsteps_, p->spec.nt);
     }
     for (auto& g : groups_) {
+        // the group's step kernel: forced, or by the measured crossover
+        if (tc_.kind == MNAD_KERNEL_DIRECT || tc_.kind == MNAD_KERNEL_TMA) g->kind = tc_.kind;
+        else g->kind = (double)g->props.size() * g->nz * g->nx < AUTO_DIRECT_MAX_POINTS ? MNAD_KERNEL_DIRECT
+                                                                                          : MNAD_KERNEL_TMA;
+        const bool tma = g->kind == MNAD_KERNEL_TMA;
+        g->ntz = tma ? (g->nz + TMA_TZ - 1) / TMA_TZ : (g->nz + DIRECT_TZ - 1) / DIRECT_TZ;
+        g->tiles_per_prop = g->ntz * (tma ? (g->nx + TMA_TX - 1) / TMA_TX : (g->nx + DIRECT_TX - 1) / DIRECT_TX);
         std::vector<PropDesc> descs;
         std::vector<int> tile_prop;
         std::vector<int4> info;
@@ -565,10 +584,10 @@ void Batch::finalize()
             Prop* p = g->props[k];
             PropDesc& D = p->desc;
             D.tile_base = (int)tile_prop.size();
-            tile_prop.insert(tile_prop.end(), (size_t)D.ntz * D.ntx, (int)k);
+            tile_prop.insert(tile_prop.end(), (size_t)g->tiles_per_prop, (int)k);
             descs.push_back(D);
             all.push_back(D);
-            if (tc_.kind != MNAD_KERNEL_TMA) continue;
+            if (!tma) continue;
             const int ncols = D.nx + 2 * HX;
             for (int t = 0; t < 2; ++t)
                 for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ + 8, TMA_TX + 4));
@@ -627,10 +646,10 @@ void Batch::launch_step(int s, int slot)
         a.tile_info = g->tile_info.as<int4>();
         a.tile_counter = d_counters_.as<int>() + (d_counters_.get() ? (size_t)slot * groups_.size() + gi : 0);
         a.ntiles = g->ntiles;
-        a.ntz = g->props.empty() ? 0 : g->props[0]->desc.ntz;
-        a.tiles_per_prop = g->props.empty() ? 0 : g->props[0]->desc.ntz * g->props[0]->desc.ntx;
+        a.ntz = g->ntz;
+        a.tiles_per_prop = g->tiles_per_prop;
         a.s = s;
-        if (tc_.kind == MNAD_KERNEL_TMA) {
+        if (g->kind == MNAD_KERNEL_TMA) {
             const size_t smem = step_tma_smem_bytes();
             const int grid = std::min(g->ntiles, ctx_.num_sms * TMA_CTAS_PER_SM);
             step_tma<<<grid, TMA_THREADS, smem, ctx_.stream>>>(a);
@@ -706,7 +725,7 @@ void Batch::refresh_descs()
         for (Prop* p : g->props) {
             PropDesc D = p->desc;
             D.tile_base = base;                 // this batch's tile numbering
-            base += D.ntz * D.ntx;
+            base += g->tiles_per_prop;
             descs.push_back(D);
             all.push_back(D);
         }
@@ -724,7 +743,7 @@ void Batch::advance(int s0, int s1)
         en |= p->energy.get() != nullptr;
         ck |= p->ckpt.saving && p->ckpt.C > 0;
     }
-    if (tc_.kind == MNAD_KERNEL_TMA && s1 > s0) {
+    if (has_tma() && s1 > s0) {
         // one tile counter per step and group, zeroed before these launches
         const size_t need = reserve_counters(s1 - s0);
         MNAD_CK(cudaMemsetAsync(d_counters_.get(), 0, need, ctx_.stream));
@@ -736,6 +755,20 @@ void Batch::advance(int s0, int s1)
         if (ck) checkpoint_after(s);
     }
     MNAD_CK(cudaGetLastError());
+}
+
+bool Batch::has_tma() const
+{
+    for (const auto& g : groups_)
+        if (g->kind == MNAD_KERNEL_TMA && g->ntiles > 0) return true;
+    return false;
+}
+
+int Batch::launches_per_step() const
+{
+    int n = 0;
+    for (const auto& g : groups_) n += g->ntiles > 0;
+    return n;
 }
 
 bool Batch::has_step_hooks() const
@@ -757,7 +790,7 @@ void Batch::tick(int K, bool use_graph)
     if (!tick_graph_ || tick_K_ != K) {
         if (tick_graph_) cudaGraphExecDestroy(tick_graph_);
         tick_graph_ = nullptr;
-        if (tc_.kind == MNAD_KERNEL_TMA) reserve_counters(K);   // allocate outside the capture
+        if (has_tma()) reserve_counters(K);   // allocate outside the capture
         cudaGraph_t g = nullptr;
         MNAD_CK(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal));
         advance(0, K);
@@ -786,7 +819,7 @@ void Batch::run(bool use_graph)
     if (!graph_) {
         // allocate outside the capture: a graph that allocates memory cannot
         // be relaunched while that memory is held
-        if (tc_.kind == MNAD_KERNEL_TMA) reserve_counters(nsteps_);
+        if (has_tma()) reserve_counters(nsteps_);
         cudaGraph_t g = nullptr;
         MNAD_CK(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal));
         body();

@@ -75,12 +75,30 @@ struct Context {
     unsigned take_status();
 };
 
-// Tile shape of a step kernel; receivers are bucketed per tile of this shape.
+// Step-kernel choice of a batch: MNAD_KERNEL_DIRECT, MNAD_KERNEL_TMA, or
+// MNAD_KERNEL_AUTO (per launch group: the direct kernel below
+// AUTO_DIRECT_MAX_POINTS point-updates per launch, the TMA kernel above).
 struct TileCfg {
-    int kind;   // MNAD_KERNEL_DIRECT / MNAD_KERNEL_TMA
-    int tz, tx;
+    int kind;
+    int tz, tx;   // receiver bucket tile: TMA_TZ x TMA_TX for every kernel
 };
 TileCfg tile_cfg(int kernel);
+// Measured crossover of the two step kernels on GB300 (grids of 48^2 to 512^2,
+// 1 and 8 propagations per launch): the persistent TMA kernel's fixed cost per
+// launch loses below about a million point-updates per launch.
+constexpr double AUTO_DIRECT_MAX_POINTS = 1.0e6;
+
+// Receivers of one propagation bucketed by TMA_TZ x TMA_TX tile and, within a
+// tile, by column (stable counting sort): entries of tile t are
+// tile_rec[t] .. tile_rec[t+1], those of its local column c are
+// col_rec[t*TMA_TX + c] .. col_rec[t*TMA_TX + c+1].  pt: storage offsets,
+// id: receiver numbers, rr: r at the receiver (mode's formula).
+struct RecBuckets {
+    std::vector<int> pt, id, tile_rec, col_rec;
+    std::vector<double> rr;
+};
+void bucket_receivers(int nz, int nx, int ld, const std::vector<int>& zr, const std::vector<int>& xr,
+                      const double* v, double dt, int mode, RecBuckets& out);
 
 // Geometry and inputs of one propagation.
 struct PropSpec {
@@ -138,8 +156,10 @@ struct LaunchGroup {
     double dx = 0, dz = 0;
     int nz = 0, nx = 0, d = 0;
     std::vector<Prop*> props;
+    int kind = MNAD_KERNEL_TMA;        // step kernel of this group
     DevMem desc, tile_prop, tmaps, tile_info;
-    int ntiles = 0;
+    int ntiles = 0;                    // tiles of one launch (of the group's kernel)
+    int ntz = 0, tiles_per_prop = 0;   // tiling of the group's kernel
 };
 
 // Propagations that advance together: one launch per geometry group and step.
@@ -158,6 +178,10 @@ public:
     // shift each propagation's s_off by -K between ticks.
     void tick(int K, bool use_graph);
     bool has_step_hooks() const;       // FP16 snapshot encodes, energy or checkpoints per step
+    bool has_tma() const;              // a group runs the TMA kernel
+    int launches_per_step() const;     // step-kernel launches of one time step
+    int group_kind(size_t g) const { return groups_[g]->kind; }
+    size_t groups() const { return groups_.size(); }
     int steps() const { return nsteps_; }
     int tiles() const { return ntiles_; }
     const std::vector<Prop*>& props() const { return props_; }

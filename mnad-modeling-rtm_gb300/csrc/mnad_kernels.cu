@@ -26,9 +26,13 @@ step_direct(const __grid_constant__ StepArgs A)
     const int tt = step_tt(P, s);
     if (tt == 0) return;
     const int tl = blockIdx.x - P.tile_base;
-    const int tz = tl % P.ntz, tx = tl / P.ntz;
-    const int j = tz * DIRECT_TZ + threadIdx.x;
-    const int i = tx * DIRECT_TX + threadIdx.y;
+    const int tz = tl % A.ntz, tx = tl / A.ntz;
+    const int j0 = tz * DIRECT_TZ, i0 = tx * DIRECT_TX;
+    const int j = j0 + threadIdx.x;
+    const int i = i0 + threadIdx.y;
+    // receiver buckets are per TMA tile and column; this tile's DIRECT_TX
+    // columns are consecutive columns of one TMA tile
+    const int cb = (j0 / TMA_TZ + (i0 / TMA_TX) * P.ntz) * TMA_TX + i0 % TMA_TX;
     const int cur = s & 1;
     const float* __restrict__ U = P.fld[cur][0];
     const float* __restrict__ V = P.fld[cur][1];
@@ -36,7 +40,7 @@ step_direct(const __grid_constant__ StepArgs A)
     float* nU = P.fld[cur ^ 1][0];
     float* nV = P.fld[cur ^ 1][1];
     float* nW = P.fld[cur ^ 1][2];
-    if (P.mode == MODE_FWD && P.nr > 0) record_receivers(P, tt, tl, U, V, W);
+    if (P.mode == MODE_FWD && P.nr > 0) record_receivers(P, tt, cb, j0, U, V, W);
     if (j >= P.nz || i >= P.nx) return;
     const int ld = P.ld;
     const size_t p = (size_t)(i + HX) * ld + (j + HZ);
@@ -56,7 +60,7 @@ step_direct(const __grid_constant__ StepArgs A)
     float su, sv, sw;
     mnad_update(K, r, h, su, sv, sw);
     float xu, xv, xw;
-    finish_point(P, tt, j, i, p, r, h, su, sv, sw, pu, pv, pw, adjoint_injection(P, tt, tl, p), xu, xv, xw);
+    finish_point(P, tt, j, i, p, r, h, su, sv, sw, pu, pv, pw, adjoint_injection(P, tt, cb + threadIdx.y, p), xu, xv, xw);
     nU[p] = xu;
     nV[p] = xv;
     nW[p] = xw;

@@ -16,6 +16,8 @@ constexpr int TMA_TZ = 64;
 constexpr int TMA_TX = 16;
 constexpr int TMA_TZY = TMA_TZ / TMA_PZ;
 constexpr int TMA_THREADS = TMA_TZY * TMA_TX;
+// Direct tiles nest in TMA tiles, so both kernels read one receiver bucketing.
+static_assert(TMA_TZ % DIRECT_TZ == 0 && TMA_TX % DIRECT_TX == 0, "direct tiles must nest in TMA tiles");
 constexpr int TMA_STAGES = 3;         // tiles in flight per CTA
 constexpr int TMA_CTAS_PER_SM = 2;
 // Tensor maps of one propagation: halo boxes of U,V,W at both time levels,

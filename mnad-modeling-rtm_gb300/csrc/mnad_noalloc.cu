@@ -66,9 +66,10 @@ size_t noalloc_bytes_needed(int nz, int nx, int d, int nt, int nr)
     const size_t S = ld * (nx + 2 * HX);
     const size_t dpz = (size_t)((d + 6 + 3) / 4 * 4);
     const size_t ntiles = (size_t)((nz + DIRECT_TZ - 1) / DIRECT_TZ) * ((nx + DIRECT_TX - 1) / DIRECT_TX);
+    const size_t nbt = (size_t)((nz + TMA_TZ - 1) / TMA_TZ) * ((nx + TMA_TX - 1) / TMA_TX);
     size_t b = 0;
     b += align256(sizeof(PropDesc)) + align256(sizeof(unsigned));
-    b += align256(ntiles * sizeof(int)) + align256((ntiles + 1) * sizeof(int));
+    b += align256(ntiles * sizeof(int)) + align256((nbt + 1) * sizeof(int)) + align256((nbt * TMA_TX + 1) * sizeof(int));
     b += align256((size_t)nr * sizeof(int)) * 2 + align256((size_t)nr * sizeof(double));
     b += align256((size_t)nt * sizeof(float));
     b += align256(6 * S * sizeof(float)) + align256(S * sizeof(float));
@@ -100,10 +101,12 @@ void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, doub
     const int dpz = (d + 6 + 3) / 4 * 4;
     const int ntz = (nz + DIRECT_TZ - 1) / DIRECT_TZ, ntx = (nx + DIRECT_TX - 1) / DIRECT_TX;
     const int ntiles = ntz * ntx;
+    const int bz = (nz + TMA_TZ - 1) / TMA_TZ, bx = (nx + TMA_TX - 1) / TMA_TX, nbt = bz * bx;
     PropDesc* d_desc = reinterpret_cast<PropDesc*>(take(sizeof(PropDesc)));
     unsigned* d_status = reinterpret_cast<unsigned*>(take(sizeof(unsigned)));
     int* d_tile_prop = reinterpret_cast<int*>(take(ntiles * sizeof(int)));
-    int* d_tile_rec = reinterpret_cast<int*>(take((ntiles + 1) * sizeof(int)));
+    int* d_tile_rec = reinterpret_cast<int*>(take((nbt + 1) * sizeof(int)));
+    int* d_col_rec = reinterpret_cast<int*>(take(((size_t)nbt * TMA_TX + 1) * sizeof(int)));
     int* d_rec_pt = reinterpret_cast<int*>(take((size_t)nr * sizeof(int)));
     int* d_rec_id = reinterpret_cast<int*>(take((size_t)nr * sizeof(int)));
     double* d_rec_r = reinterpret_cast<double*>(take((size_t)nr * sizeof(double)));
@@ -118,19 +121,11 @@ void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, doub
     }
     double* d_data = reinterpret_cast<double*>(take((size_t)nt * nr * sizeof(double)));
 
-    // Host-side tables: receivers bucketed per tile, source amplitudes.
+    // Host-side tables: receivers bucketed per tile and column, source amplitudes.
     auto at = [&](int j, int i) { return (int)((size_t)(i + HX) * ld + (j + HZ)); };
-    std::vector<int> cnt(ntiles + 1, 0), pt(nr), id(nr), zero(ntiles, 0);
-    std::vector<double> rr(nr);
-    for (int k = 0; k < nr; ++k) cnt[1 + zr[k] / DIRECT_TZ + (xr[k] / DIRECT_TX) * ntz]++;
-    for (int t = 0; t < ntiles; ++t) cnt[t + 1] += cnt[t];
-    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-    for (int k = 0; k < nr; ++k) {
-        const int e = fill[zr[k] / DIRECT_TZ + (xr[k] / DIRECT_TX) * ntz]++;
-        pt[e] = at(zr[k], xr[k]);
-        id[e] = k;
-        rr[e] = r_of(v[(size_t)zr[k] + (size_t)xr[k] * nz], dt, MODE_FWD);
-    }
+    std::vector<int> zero(ntiles, 0);
+    RecBuckets rb;
+    bucket_receivers(nz, nx, ld, zr, xr, v, dt, MODE_FWD, rb);
     std::vector<float> amp(nt);
     const double rs = r_of(v[(size_t)zs + (size_t)xs * nz], dt, MODE_FWD);
     for (int t = 0; t < nt; ++t) amp[t] = (float)(rs * w[t]);
@@ -139,7 +134,7 @@ void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, doub
     std::memset(&D, 0, sizeof(D));
     D.s_begin = INT_MIN; D.s_end = INT_MAX;
     D.mode = MODE_FWD; D.nt = nt; D.nz = nz; D.nx = nx; D.ld = ld; D.d = d; D.dpz = dpz; D.zb0 = (nz - d) & ~3;
-    D.ntz = ntz; D.ntx = ntx; D.tile_base = 0;
+    D.ntz = bz; D.ntx = bx; D.tile_base = 0;
     for (int t = 0; t < 2; ++t)
         for (int f = 0; f < 3; ++f) D.fld[t][f] = d_fields + (size_t)(t * 3 + f) * S;
     D.r = d_r; D.mx = d_mx; D.mz = d_mz;
@@ -152,6 +147,7 @@ void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, doub
     D.inv_dt2 = (float)(1.0 / (dt * dt));
     D.src = at(zs, xs); D.src_amp = d_amp;
     D.nr = nr; D.rec_pt = d_rec_pt; D.rec_id = d_rec_id; D.rec_r = d_rec_r; D.tile_rec = d_tile_rec;
+    D.col_rec = d_col_rec;
     D.data = d_data;
     D.status = d_status;
 
@@ -172,11 +168,13 @@ void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, doub
     MNAD_CK(cudaMemsetAsync(d_status, 0, sizeof(unsigned), st));
     MNAD_CK(cudaMemcpyAsync(d_desc, &D, sizeof(D), cudaMemcpyHostToDevice, st));
     MNAD_CK(cudaMemcpyAsync(d_tile_prop, zero.data(), ntiles * sizeof(int), cudaMemcpyHostToDevice, st));
-    MNAD_CK(cudaMemcpyAsync(d_tile_rec, cnt.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    MNAD_CK(cudaMemcpyAsync(d_tile_rec, rb.tile_rec.data(), (nbt + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    MNAD_CK(cudaMemcpyAsync(d_col_rec, rb.col_rec.data(), ((size_t)nbt * TMA_TX + 1) * sizeof(int),
+                            cudaMemcpyHostToDevice, st));
     if (nr > 0) {
-        MNAD_CK(cudaMemcpyAsync(d_rec_pt, pt.data(), nr * sizeof(int), cudaMemcpyHostToDevice, st));
-        MNAD_CK(cudaMemcpyAsync(d_rec_id, id.data(), nr * sizeof(int), cudaMemcpyHostToDevice, st));
-        MNAD_CK(cudaMemcpyAsync(d_rec_r, rr.data(), nr * sizeof(double), cudaMemcpyHostToDevice, st));
+        MNAD_CK(cudaMemcpyAsync(d_rec_pt, rb.pt.data(), nr * sizeof(int), cudaMemcpyHostToDevice, st));
+        MNAD_CK(cudaMemcpyAsync(d_rec_id, rb.id.data(), nr * sizeof(int), cudaMemcpyHostToDevice, st));
+        MNAD_CK(cudaMemcpyAsync(d_rec_r, rb.rr.data(), nr * sizeof(double), cudaMemcpyHostToDevice, st));
     }
     MNAD_CK(cudaMemcpyAsync(d_amp, amp.data(), nt * sizeof(float), cudaMemcpyHostToDevice, st));
 
@@ -185,6 +183,9 @@ void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, doub
     stencil_polys(dx, dz, a.coef.alpha, a.coef.beta);
     a.props = d_desc;
     a.tile_prop = d_tile_prop;
+    a.ntiles = ntiles;
+    a.ntz = ntz;
+    a.tiles_per_prop = ntiles;
     for (int s = 0; s < nt; ++s) {
         a.s = s;
         step_direct<<<ntiles, dim3(DIRECT_TZ, DIRECT_TX), 0, st>>>(a);

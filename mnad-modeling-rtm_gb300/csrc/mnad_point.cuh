@@ -2,6 +2,7 @@
 // source/receivers, snapshots and imaging).
 #pragma once
 #include "mnad_device.cuh"
+#include "mnad_kernels.h"
 
 namespace mnad {
 
@@ -165,14 +166,18 @@ __device__ __forceinline__ void finish_point(const PropDesc& P, int tt, int j, i
 
 // Forward receivers: datau(tt,rr) = U(zr,xr) after the injection and before
 // the update (fwd_PDE_exact_MNAD.m:119-123).  Stored U holds exactly that.
-__device__ __forceinline__ void record_receivers(const PropDesc& P, int tt, int tl,
+// The block records the entries of the DIRECT_TX bucket columns from `cb`
+// whose row lies in its DIRECT_TZ rows from j0.
+__device__ __forceinline__ void record_receivers(const PropDesc& P, int tt, int cb, int j0,
     const float* U, const float* V, const float* W)
 {
-    const int beg = __ldg(P.tile_rec + tl), end = __ldg(P.tile_rec + tl + 1);
+    const int beg = __ldg(P.col_rec + cb), end = __ldg(P.col_rec + cb + DIRECT_TX);
     const int tid = threadIdx.x + threadIdx.y * blockDim.x;
     const int nth = blockDim.x * blockDim.y;
     for (int k = beg + tid; k < end; k += nth) {
         const int pt = __ldg(P.rec_pt + k);
+        const int row = pt % P.ld - HZ;
+        if (row < j0 || row >= j0 + DIRECT_TZ) continue;
         const size_t o = (size_t)__ldg(P.rec_id + k) * P.nt + (tt - 1);
         const float u = U[pt];
         if (!isfinite(u)) atomicOr(P.status, ST_NONFINITE);
@@ -182,13 +187,13 @@ __device__ __forceinline__ void record_receivers(const PropDesc& P, int tt, int 
     }
 }
 
-// Adjoint receiver injection r*data(tt+1) summed over the entries of tile
-// `tl` that sit at storage offset p (duplicated receivers add up).
-__device__ __forceinline__ float adjoint_injection(const PropDesc& P, int tt, int tl, size_t p)
+// Adjoint receiver injection r*data(tt+1) summed over the entries of bucket
+// column `c` that sit at storage offset p (duplicated receivers add up).
+__device__ __forceinline__ float adjoint_injection(const PropDesc& P, int tt, int c, size_t p)
 {
     float inj = 0.0f;
     if (P.mode != MODE_ADJ || tt >= P.nt) return inj;
-    const int beg = __ldg(P.tile_rec + tl), end = __ldg(P.tile_rec + tl + 1);
+    const int beg = __ldg(P.col_rec + c), end = __ldg(P.col_rec + c + 1);
     for (int k = beg; k < end; ++k)
         if (__ldg(P.rec_pt + k) == (int)p) {
             const int rr = __ldg(P.rec_id + k);

@@ -83,3 +83,67 @@ def test_field_offsets_of_active_groups_stay_in_the_column(nz, nx):
         assert j + HZ - 2 >= 0 and j + HZ + 3 + 2 < ld
     # halo columns +-2 of every column stay inside nx + 2*HX columns
     assert (nx - 1) + HX + 2 < nx + 2 * HX
+
+
+DIRECT_TZ, DIRECT_TX = 32, 8
+
+
+def bucket_receivers(nz, nx, zr, xr):
+    """The engine's receiver bucketing (per TMA tile, then per local column;
+    stable counting sort): returns (tile_rec, col_rec, pt, id)."""
+    ld = round_up(nz + HZ + HZB, 32)
+    ntz, ntx = -(-nz // TMA_TZ), -(-nx // TMA_TX)
+    nb = ntz * ntx * TMA_TX
+    bucket = [((z // TMA_TZ) + (x // TMA_TX) * ntz) * TMA_TX + x % TMA_TX for z, x in zip(zr, xr)]
+    cnt = [0] * (nb + 1)
+    for b in bucket:
+        cnt[b + 1] += 1
+    for b in range(nb):
+        cnt[b + 1] += cnt[b]
+    fill = cnt[:-1]
+    pt, ident = [0] * len(zr), [0] * len(zr)
+    for k, b in enumerate(bucket):
+        e = fill[b]
+        fill[b] += 1
+        pt[e] = (xr[k] + HX) * ld + (zr[k] + HZ)
+        ident[e] = k
+    tile_rec = [cnt[t * TMA_TX] for t in range(ntz * ntx + 1)]
+    return tile_rec, cnt, pt, ident, ld, ntz
+
+
+@pytest.mark.parametrize("nz,nx,nr,seed", [(48, 64, 40, 0), (37, 70, 200, 1), (201, 201, 500, 2), (66, 47, 1, 3),
+                                           (130, 35, 0, 4), (481, 1281, 900, 5)])
+def test_direct_kernel_finds_each_receiver_once_in_the_shared_buckets(nz, nx, nr, seed):
+    """Replays the direct kernel's lookup: a DIRECT_TZ x DIRECT_TX block
+    scans the DIRECT_TX bucket columns of its TMA tile and keeps the rows it
+    owns (forward recording), and a point scans its own column (adjoint
+    injection).  Every receiver, duplicates included, is found exactly once by
+    each, and every bucket index stays inside the arrays."""
+    import random
+    rnd = random.Random(seed)
+    zr = [rnd.randrange(nz) for _ in range(nr)]
+    xr = [rnd.randrange(nx) for _ in range(nr)]
+    if nr > 3:
+        zr[1], xr[1] = zr[0], xr[0]          # a duplicated receiver
+    tile_rec, col_rec, pt, ident, ld, bntz = bucket_receivers(nz, nx, zr, xr)
+    dntz, dntx = -(-nz // DIRECT_TZ), -(-nx // DIRECT_TX)
+    recorded, injected = [], []
+    for tl in range(dntz * dntx):
+        tz, tx = tl % dntz, tl // dntz
+        j0, i0 = tz * DIRECT_TZ, tx * DIRECT_TX
+        cb = (j0 // TMA_TZ + (i0 // TMA_TX) * bntz) * TMA_TX + i0 % TMA_TX
+        assert 0 <= cb and cb + DIRECT_TX < len(col_rec)
+        for k in range(col_rec[cb], col_rec[cb + DIRECT_TX]):
+            row = pt[k] % ld - HZ
+            if j0 <= row < j0 + DIRECT_TZ:
+                recorded.append(ident[k])
+        for ty in range(DIRECT_TX):
+            for tzt in range(DIRECT_TZ):
+                j, i = j0 + tzt, i0 + ty
+                if j >= nz or i >= nx:
+                    continue
+                p = (i + HX) * ld + (j + HZ)
+                c = cb + ty
+                injected += [ident[k] for k in range(col_rec[c], col_rec[c + 1]) if pt[k] == p]
+    assert sorted(recorded) == list(range(nr))
+    assert sorted(injected) == list(range(nr))
