@@ -64,8 +64,8 @@ __device__ __forceinline__ void cpml_point(const PropDesc& P, int j, int i, floa
     }
     if (j < d || j >= P.nz - d) {
         const int side = j < d ? 0 : 1;
-        const int k = side ? j - P.zb0 : j;
-        const float X = side ? float(k + 1) * P.dz : float(d - j) * P.dz;
+        const int k = side ? j - P.zb0 : j;      // storage slot (zb0 is nz - d rounded down to 4)
+        const float X = side ? float(j - (P.nz - d) + 1) * P.dz : float(d - j) * P.dz;
         float c1, c2, c3;
         cpml_coefs(P.kz, vel, X, P.dt, c1, c2, c3);
         const float inv_h = 1.0f / P.dz;

@@ -1,6 +1,7 @@
 """Edge cases of the hot path against the FP64 C oracle: a source inside the
 CPML strip next to a corner (the strip's pre-injection correction),
-receivers in the strip, a snapshot at every step (T = 1, so the d2u of
+receivers in the strip, a bottom strip whose rows are off the 4-row storage
+grid, a snapshot at every step (T = 1, so the d2u of
 tt = 1 and tt = 2 take the reference's special forms), the shortest records
 (nt = 1, 2) and a shot without receivers."""
 import numpy as np
@@ -45,6 +46,28 @@ def test_source_in_the_cpml_strip(ctx, kernel, zs, xs):
     finally:
         ctx.set_options(kernel="auto")
     ref = coracle.fwd(10.0, xs, xr, 10.0, zs, zr, v, 1e-3, nt, w, d)["datau"]
+    assert rel(out, ref) <= 1e-5
+    assert ctx.status() == 0
+
+
+@pytest.mark.parametrize("kernel", ["direct", "tma"])
+@pytest.mark.parametrize("nz", [53, 54, 55])
+def test_bottom_strip_when_nz_minus_d_is_not_a_multiple_of_4(ctx, kernel, nz):
+    """The bottom z strip's memory variables are stored from row nz - d
+    rounded down to 4; the damping profile still starts at row nz - d.  A
+    source just above the strip and receivers inside it see the difference
+    within a few wave periods."""
+    v = _model(nz=nz)
+    d, nt = 8, 220
+    w = workflow.ricker(30.0, 1e-3, nt)
+    xr = np.array([10, 20, 30, 40, 50, 30, 30], dtype=float)
+    zr = np.array([nz - 9, nz - 7, nz - 5, nz - 3, nz - 1, nz, nz - 10], dtype=float)
+    ctx.set_options(kernel=kernel)
+    try:
+        out = ctx.fwd(10.0, 30, xr, 10.0, nz - d - 2, zr, v, 1e-3, nt, w, d)
+    finally:
+        ctx.set_options(kernel="auto")
+    ref = coracle.fwd(10.0, 30, xr, 10.0, nz - d - 2, zr, v, 1e-3, nt, w, d)["datau"]
     assert rel(out, ref) <= 1e-5
     assert ctx.status() == 0
 
