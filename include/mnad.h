@@ -270,6 +270,7 @@ typedef struct mnad_server_stats {
     double busy_s;                  /* worker time spent in ticks */
     double wall_s;                  /* since the first submission */
     size_t bytes_in_use;            /* device memory held by the server now */
+    size_t peak_bytes;              /* largest device memory the server has held */
 } mnad_server_stats;
 
 MNAD_API int mnad_server_create(int device, const mnad_server_options* opt, mnad_server** out);

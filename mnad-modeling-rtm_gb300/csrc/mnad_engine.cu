@@ -83,6 +83,7 @@ void* Context::alloc(size_t bytes)
     void* p = nullptr;
     MNAD_CK(cudaMallocAsync(&p, bytes, stream));
     in_use += bytes;
+    peak = std::max(peak, in_use);
     return p;
 }
 

@@ -61,6 +61,7 @@ struct Context {
     mnad_options opt{};
     size_t budget = 0;        // 0: unbounded
     size_t in_use = 0;
+    size_t peak = 0;           // largest in_use since creation
     uint64_t h2d = 0, d2h = 0;   // bytes copied host->device / device->host
     int num_sms = 0;
     unsigned* d_status = nullptr;

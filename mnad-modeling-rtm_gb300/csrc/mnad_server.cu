@@ -77,6 +77,7 @@ struct mnad_server {
     std::unique_ptr<Batch> batch;
     size_t budget = 0, reserve = 0;          // HBM budget; part kept for batch tables
     std::atomic<size_t> mem_in_use{0};       // the context's device bytes, for other threads
+    std::atomic<size_t> mem_peak{0};         // the context's largest device bytes so far
     bool dirty = true;
     // Each tick runs global steps 0..K-1; a propagation's local step at tick
     // step s is s - s_off, and s_off drops by K after every tick.
@@ -226,6 +227,7 @@ void mnad_server::loop()
             }
             const bool admitted = admit(j);
             mem_in_use.store(std::max(mem_in_use.load(), ctx->in_use));
+            mem_peak.store(ctx->peak);
             if (!admitted) break;            // not enough memory yet: keep FIFO order
             std::lock_guard<std::mutex> lk(mu);
             queue.pop_front();
@@ -283,6 +285,7 @@ void mnad_server::loop()
             dirty = true;
         }
         mem_in_use.store(ctx->in_use);
+        mem_peak.store(ctx->peak);
         std::lock_guard<std::mutex> lk(mu);
         busy_s += std::chrono::duration<double>(Clock::now() - t0).count();
     }
@@ -426,6 +429,7 @@ MNAD_API int mnad_server_get_stats(mnad_server* S, mnad_server_stats* st)
         st->busy_s = S->busy_s;
         st->wall_s = S->any_submit ? std::chrono::duration<double>(Clock::now() - S->t_first_submit).count() : 0.0;
         st->bytes_in_use = S->mem_in_use.load();
+        st->peak_bytes = S->mem_peak.load();
     });
 }
 

@@ -51,7 +51,7 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
                 ("point_updates", C.c_double), ("busy_s", C.c_double), ("wall_s", C.c_double),
-                ("bytes_in_use", C.c_size_t)]
+                ("bytes_in_use", C.c_size_t), ("peak_bytes", C.c_size_t)]
 
 
 SIGNATURES = {

@@ -136,7 +136,9 @@ def test_admission_by_hbm_budget_and_oversized_jobs():
         with pytest.raises(mnad.MnadError) as e:
             srv.wait(t_huge, timeout_s=300)
         assert e.value.code == mnad._lib.E_BUDGET
-    assert max(seen) <= budget
+        peak = srv.stats()["peak_bytes"]
+    assert max(seen, default=0) <= budget
+    assert 0 < peak <= budget
     for a, b in zip(jobs, ref):
         _same(a, b)
 
