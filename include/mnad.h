@@ -63,8 +63,9 @@ enum { MNAD_SNAP_F32 = 0, MNAD_SNAP_BF16 = 1, MNAD_SNAP_F16 = 2 };
 enum { MNAD_PAIR_REFERENCE = 0, MNAD_PAIR_ALIGNED = 1 };
 
 /* Step kernel choice.  AUTO picks per launch group (propagations of one grid
- * size advancing together): the one-thread-per-point kernel below a million
- * point-updates per launch, the persistent TMA kernel above. */
+ * size advancing together): the persistent TMA kernel once a launch has about
+ * 2.25 of its 64 x 16 tiles per resident CTA (0.7M point-updates on a
+ * 152-SM GB300), the one-thread-per-point kernel below. */
 enum { MNAD_KERNEL_AUTO = 0, MNAD_KERNEL_DIRECT = 1, MNAD_KERNEL_TMA = 2 };
 
 typedef struct mnad_options {

@@ -572,8 +572,12 @@ void Batch::finalize()
     for (auto& g : groups_) {
         // the group's step kernel: forced, or by the measured crossover
         if (tc_.kind == MNAD_KERNEL_DIRECT || tc_.kind == MNAD_KERNEL_TMA) g->kind = tc_.kind;
-        else g->kind = (double)g->props.size() * g->nz * g->nx < AUTO_DIRECT_MAX_POINTS ? MNAD_KERNEL_DIRECT
-                                                                                          : MNAD_KERNEL_TMA;
+        else {
+            const double tiles = (double)g->props.size() * ((g->nz + TMA_TZ - 1) / TMA_TZ) *
+                                 ((g->nx + TMA_TX - 1) / TMA_TX);
+            g->kind = tiles >= AUTO_TMA_TILES_PER_CTA * ctx_.num_sms * TMA_CTAS_PER_SM ? MNAD_KERNEL_TMA
+                                                                                      : MNAD_KERNEL_DIRECT;
+        }
         const bool tma = g->kind == MNAD_KERNEL_TMA;
         g->ntz = tma ? (g->nz + TMA_TZ - 1) / TMA_TZ : (g->nz + DIRECT_TZ - 1) / DIRECT_TZ;
         g->tiles_per_prop = g->ntz * (tma ? (g->nx + TMA_TX - 1) / TMA_TX : (g->nx + DIRECT_TX - 1) / DIRECT_TX);

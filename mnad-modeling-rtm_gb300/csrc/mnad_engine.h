@@ -77,17 +77,20 @@ struct Context {
 };
 
 // Step-kernel choice of a batch: MNAD_KERNEL_DIRECT, MNAD_KERNEL_TMA, or
-// MNAD_KERNEL_AUTO (per launch group: the direct kernel below
-// AUTO_DIRECT_MAX_POINTS point-updates per launch, the TMA kernel above).
+// MNAD_KERNEL_AUTO (per launch group: the TMA kernel once a launch has
+// AUTO_TMA_TILES_PER_CTA of its tiles for each resident CTA, the direct
+// kernel below).
 struct TileCfg {
     int kind;
     int tz, tx;   // receiver bucket tile: TMA_TZ x TMA_TX for every kernel
 };
 TileCfg tile_cfg(int kernel);
-// Measured crossover of the two step kernels on GB300 (grids of 48^2 to 512^2,
-// 1 and 8 propagations per launch): the persistent TMA kernel's fixed cost per
-// launch loses below about a million point-updates per launch.
-constexpr double AUTO_DIRECT_MAX_POINTS = 1.0e6;
+// Measured crossover of the two step kernels on GB300 (152 SMs, 2 CTAs per
+// SM; grids of 96^2 to 2048^2, 1 to 8 propagations per launch): the direct
+// kernel wins up to 0.59M point-updates per launch (575 tiles, 1.9 per CTA),
+// the persistent TMA kernel from 0.82M (800 tiles, 2.6 per CTA) on; its
+// pipeline needs a few tiles per CTA to hide the load latency.
+constexpr double AUTO_TMA_TILES_PER_CTA = 2.25;
 
 // Receivers of one propagation bucketed by TMA_TZ x TMA_TX tile and, within a
 // tile, by column (stable counting sort): entries of tile t are

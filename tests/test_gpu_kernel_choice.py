@@ -1,8 +1,8 @@
 """GPU tests of the per-launch-group step-kernel choice (MNAD_KERNEL_AUTO).
 
-A plan whose propagations fall into a small launch group (under a million
-point-updates per launch: the direct kernel) and a large one (the TMA kernel)
-must give, group by group, bitwise the outputs of the kernel the policy
+A plan whose propagations fall into a small launch group (fewer than 2.25
+TMA tiles of 64 x 16 points per resident CTA: the direct kernel) and a large
+one (the TMA kernel) must give, group by group, bitwise the outputs of the kernel the policy
 picks when that kernel is forced for the whole plan.  Both forced runs are
 also checked against the FP64 oracle on one shot of each group."""
 import numpy as np
@@ -52,8 +52,8 @@ def _run(kernel, small, large):
 
 
 def test_auto_picks_the_kernel_per_launch_group():
-    small = _jobs(96, 112, 3, 160, 1)             # 3 x 96 x 112 = 32k points per launch
-    large = _jobs(360, 376, 8, 160, 2)            # 8 x 360 x 376 = 1.08M points per launch
+    small = _jobs(96, 112, 3, 160, 1)             # 42 tiles per launch
+    large = _jobs(360, 376, 8, 160, 2)            # 1152 tiles per launch (>= 2.25 x 304 CTAs)
     ns = len(small)
     auto = _run("auto", small, large)
     direct = _run("direct", small, large)
