@@ -307,11 +307,15 @@ def run_ours(args):
     sampler = ClockSampler(local)
     sampler.start()
     run_ms, step_ms = [], []
+    phase_ms = [0.0, 0.0]
     launches = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         plan.run()
         tm = plan.timing()
+        ph = plan.phases()
+        phase_ms[0] += ph["forward_ms"]
+        phase_ms[1] += ph["adjoint_ms"]
         run_ms.append(tm["run_ms"])
         step_ms.append(tm["step_ms"])
         launches += tm["step_launches"] + 2 + len(jobs)   # step kernels + source seeding + residuals
@@ -336,6 +340,13 @@ def run_ours(args):
             "peak_kind": f"{peak_kind} hbm_gbs",
             "kernel": "mnad::step_direct" if args.kernel == "direct" else "mnad::step_tma",
             "algorithmic_bytes_per_launch": abytes / plan.timing()["step_launches"]}
+    # the same roofline split by phase (forwards with snapshots; adjoints with imaging)
+    ph = plan.phases()
+    roof["phases"] = {
+        name: {"ms_per_step": round(ms / args.steps, 1),
+               "achieved": round(b * args.steps / (ms / 1e3) / 1e9, 1) if ms > 0 else None,
+               "frac": round(b * args.steps / (ms / 1e3) / 1e9 / peak, 4) if ms > 0 else None}
+        for name, ms, b in (("forward", phase_ms[0], ph["forward_bytes"]), ("adjoint", phase_ms[1], ph["adjoint_bytes"]))}
     # the one exchange of the path: the FP64 image / illumination stack over ranks
     t = time.perf_counter()
     im, il, _ = plan.stack()

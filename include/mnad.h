@@ -230,6 +230,11 @@ MNAD_API int mnad_plan_work(const mnad_plan* plan, double* point_updates, double
 /* Device time of the last run (ms, CUDA events on the plan's stream) and the
  * device time spent in step kernels only. */
 MNAD_API int mnad_plan_timing(const mnad_plan* plan, double* run_ms, double* step_ms, int* step_launches);
+/* The last run split by phase: device time (ms) and algorithmic bytes of the
+ * forwards (phase 1) and of the adjoints (phase 3; with checkpointing this
+ * phase also holds the background recomputation). */
+MNAD_API int mnad_plan_phases(const mnad_plan* plan, double* forward_ms, double* forward_bytes, double* adjoint_ms,
+                              double* adjoint_bytes);
 /* Stack of the plan's RTM shots after mnad_plan_run, formed in FP64 on the
  * device (SRC/migration/main_Acoustic_RTM.m:237-262): image_sum = sum of the
  * shots' images (each T*sum US.*UR), illum_sum = sum of the shots'

@@ -414,7 +414,8 @@ struct mnad_plan {
     std::unique_ptr<Batch> recomp;
     cudaEvent_t ev[4] = {};
     double pts = 0, bytes = 0;
-    float run_ms = 0, step_ms = 0;
+    double bytes_fwd = 0, bytes_adj = 0;        // phase 1 / phase 3 (with the recomputation)
+    float run_ms = 0, step_ms = 0, fwd_ms = 0, adj_ms = 0;
     int launches = 0;
     ~mnad_plan()
     {
@@ -575,6 +576,7 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
             (p->spec.mode == MODE_FWD ? P->phase1 : P->phase3)->add(p.get());
             P->pts += p->point_updates();
             P->bytes += p->algorithmic_bytes();
+            (p->spec.mode == MODE_FWD ? P->bytes_fwd : P->bytes_adj) += p->algorithmic_bytes();
         }
         if (P->ckpt)
             for (int k = 0; k < njobs; ++k) {
@@ -586,6 +588,7 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
                 P->recomp->add(b);
                 P->pts += b->point_updates();           // the recomputation is work done too
                 P->bytes += b->algorithmic_bytes();
+                P->bytes_adj += b->algorithmic_bytes();
             }
         if (P->ckpt) P->recomp->finalize();
         P->phase1->finalize();
@@ -626,6 +629,8 @@ MNAD_API int mnad_plan_run(mnad_plan* P)
         MNAD_CK(cudaEventElapsedTime(&b, P->ev[2], P->ev[3]));
         P->run_ms = t;
         P->step_ms = a + b;
+        P->fwd_ms = a;
+        P->adj_ms = b;
         P->launches = P->phase1->steps() + (P->ckpt ? seg_launches : P->phase3->steps());
     });
 }
@@ -689,6 +694,18 @@ MNAD_API int mnad_plan_timing(const mnad_plan* P, double* run_ms, double* step_m
         if (run_ms) *run_ms = P->run_ms;
         if (step_ms) *step_ms = P->step_ms;
         if (launches) *launches = P->launches;
+    });
+}
+
+MNAD_API int mnad_plan_phases(const mnad_plan* P, double* forward_ms, double* forward_bytes, double* adjoint_ms,
+                              double* adjoint_bytes)
+{
+    return guard([&] {
+        need(P != nullptr, "plan is NULL");
+        if (forward_ms) *forward_ms = P->fwd_ms;
+        if (forward_bytes) *forward_bytes = P->bytes_fwd;
+        if (adjoint_ms) *adjoint_ms = P->adj_ms;
+        if (adjoint_bytes) *adjoint_bytes = P->bytes_adj;
     });
 }
 

@@ -308,6 +308,14 @@ class Plan:
         check(lib().mnad_plan_timing(self._h, C.byref(r), C.byref(s), C.byref(n)))
         return {"run_ms": r.value, "step_ms": s.value, "step_launches": n.value}
 
+    def phases(self):
+        """Device time (ms) and algorithmic bytes of the last run's forward
+        phase and adjoint phase."""
+        v = [C.c_double() for _ in range(4)]
+        check(lib().mnad_plan_phases(self._h, *[C.byref(x) for x in v]))
+        return {"forward_ms": v[0].value, "forward_bytes": v[1].value, "adjoint_ms": v[2].value,
+                "adjoint_bytes": v[3].value}
+
     def stack(self):
         """(image_sum, illum_sum, img_rtm) of the RTM shots, (nz-2d, nx-2d) arrays."""
         rtm = [j for j in self.jobs if j.kind == "rtm"]
