@@ -156,9 +156,11 @@ def config3(seed: int = 0, nshots: int = 64, nt: int = 4000, codec: str = "bf16"
 
 def faulted_model(nz: int, nx: int, h: float, rng, nfaults: int = 6) -> np.ndarray:
     """Seeded faulted sedimentary model: 10-16 layers whose velocities rise
-    with depth from 1500 to about 4000 m/s (gently undulating interfaces),
-    ``nfaults`` normal faults (60-70 degree dip, 40-200 m throw, hanging wall
-    down) and a salt-like 4500 m/s body; clipped to 1500-4500 m/s."""
+    with depth from 1500 to about 4000 m/s (gently undulating interfaces; the
+    first at 2-4 % of the depth, the others within the upper 60 %, so that a
+    record of a few seconds sees reflections), ``nfaults`` normal faults
+    (60-70 degree dip, 40-200 m throw, hanging wall down) and a salt-like
+    4500 m/s body at 30-45 % of the depth; clipped to 1500-4500 m/s."""
     z = np.arange(nz, dtype=np.float64)[:, None] * h
     x = np.arange(nx, dtype=np.float64)[None, :] * h
     zmax, xmax = nz * h, nx * h
@@ -171,13 +173,13 @@ def faulted_model(nz: int, nx: int, h: float, rng, nfaults: int = 6) -> np.ndarr
         hanging = (x - x0) * np.sign(dip) > (z / np.tan(abs(dip)))
         zl -= throw * hanging
     nl = int(rng.integers(10, 17))
-    tops = np.sort(rng.uniform(0.03, 0.95, nl - 1)) * zmax
+    tops = np.sort(np.concatenate(([rng.uniform(0.02, 0.04)], rng.uniform(0.04, 0.6, nl - 2)))) * zmax
     vel = np.sort(rng.uniform(1500.0, 4000.0, nl))
     vel[0] = 1500.0
     und = 0.01 * zmax * np.sin(2 * np.pi * x / rng.uniform(0.2, 0.6) / xmax + rng.uniform(0, 2 * np.pi))
     V = vel[np.searchsorted(tops, zl + und, side="right")]
     # salt body: an ellipse with a rough top
-    cz, cx = rng.uniform(0.45, 0.7) * zmax, rng.uniform(0.3, 0.7) * xmax
+    cz, cx = rng.uniform(0.3, 0.45) * zmax, rng.uniform(0.3, 0.7) * xmax
     az, ax = rng.uniform(0.08, 0.15) * zmax, rng.uniform(0.06, 0.12) * xmax
     rough = 1.0 + 0.15 * np.sin(5 * np.pi * x / xmax + rng.uniform(0, 2 * np.pi))
     V = np.where(((z - cz) / (az * rough)) ** 2 + ((x - cx) / ax) ** 2 < 1.0, 4500.0, V)
