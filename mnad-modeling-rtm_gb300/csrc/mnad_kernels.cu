@@ -12,7 +12,7 @@
 
 namespace mnad {
 
-__global__ void __launch_bounds__(DIRECT_TZ * DIRECT_TX)
+__global__ void __launch_bounds__(DIRECT_TZ * DIRECT_TX, 3)
 step_direct(const __grid_constant__ StepArgs A)
 {
     const Coefs& K = A.coef;

@@ -50,11 +50,16 @@ __device__ __forceinline__ void cpml_point(const PropDesc& P, int j, int i, floa
         const size_t vs = (size_t)d * P.ld;
         float* m = P.mx + ((size_t)(side * 9) * d + k) * P.ld + j;
         const float Fa[3] = {uxp, vxp, wxp}, Fd[3] = {uxm, vxm, wxm}, F0[3] = {u0, v0, w0};
+        // every load before the first store (the stores could alias them as
+        // far as the compiler knows, which would serialise the three fields)
+        float mv[9];
+#pragma unroll
+        for (int v = 0; v < 9; ++v) mv[v] = m[(size_t)v * vs];
         float out[3];
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             float* mf = m + (size_t)(f * 3) * vs;
-            float m1 = mf[0], m2 = mf[vs], m3 = mf[2 * vs];
+            float m1 = mv[3 * f], m2 = mv[3 * f + 1], m3 = mv[3 * f + 2];
             const float gr = side ? Fa[f] - Fd[f] : Fd[f] - Fa[f];
             const float lap = (Fd[f] + Fa[f]) - 2.0f * F0[f];
             out[f] = cpml_mem(c1, c2, c3, inv_h, gr, lap, m1, m2, m3);
@@ -72,11 +77,16 @@ __device__ __forceinline__ void cpml_point(const PropDesc& P, int j, int i, floa
         const size_t vs = (size_t)P.nx * P.dpz;
         float* m = P.mz + ((size_t)(side * 9) * P.nx + i) * P.dpz + k;
         const float Fa[3] = {uzp, vzp, wzp}, Fd[3] = {uzm, vzm, wzm}, F0[3] = {u0, v0, w0};
+        // every load before the first store (the stores could alias them as
+        // far as the compiler knows, which would serialise the three fields)
+        float mv[9];
+#pragma unroll
+        for (int v = 0; v < 9; ++v) mv[v] = m[(size_t)v * vs];
         float out[3];
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             float* mf = m + (size_t)(f * 3) * vs;
-            float m1 = mf[0], m2 = mf[vs], m3 = mf[2 * vs];
+            float m1 = mv[3 * f], m2 = mv[3 * f + 1], m3 = mv[3 * f + 2];
             const float gr = side ? Fa[f] - Fd[f] : Fd[f] - Fa[f];
             const float lap = (Fd[f] + Fa[f]) - 2.0f * F0[f];
             out[f] = cpml_mem(c1, c2, c3, inv_h, gr, lap, m1, m2, m3);

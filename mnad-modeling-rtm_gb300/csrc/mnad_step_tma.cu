@@ -370,6 +370,30 @@ __device__ __forceinline__ void cpml_c(float K, float vel, float X, float dt, fl
     c3 = (sig * dt) * inv;
 }
 
+// L2 prefetch of the memory variables that cpml_vec will read and write for
+// the TMA_PZ points j.. of column i: issued when a general tile starts, so
+// that their DRAM latency overlaps the stencil arithmetic.
+__device__ __forceinline__ void prefetch_strip_state(const PropDesc& P, int j, int i)
+{
+    constexpr int Q = TMA_PZ;
+    const int d = P.d, nz = P.nz, nx = P.nx, ld = P.ld;
+    if (i < d || i >= nx - d) {
+        const int side = i < d ? 0 : 1;
+        const int kx = side ? i - (nx - d) : i;
+        const float* m = P.mx + ((side * 9) * d + kx) * ld + j;
+#pragma unroll
+        for (int v = 0; v < 9; ++v) asm volatile("prefetch.global.L2 [%0];" ::"l"(m + v * (d * ld)));
+    }
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        if (side == 0 ? !(j < d) : !(j + Q - 1 >= nz - d)) continue;
+        const int k0 = side ? j - P.zb0 : j;
+        const float* m = P.mz + ((side * 9) * nx + i) * P.dpz + k0;
+#pragma unroll
+        for (int v = 0; v < 9; ++v) asm volatile("prefetch.global.L2 [%0];" ::"l"(m + v * (nx * P.dpz)));
+    }
+}
+
 // Ux123_gen.m / Uz123_gen.m for the TMA_PZ points j.. of column i (one
 // thread), vectorized over the points: the memory variables of a field and
 // side are TMA_PZ consecutive, aligned floats.  Adds F1_x + F1_z of
@@ -397,6 +421,11 @@ __device__ __forceinline__ void cpml_vec(const PropDesc& P, const Stage& st, int
         for (int k = 0; k < Q; ++k) cpml_c(P.kx, vel[k], X, P.dt, c1[k], c2[k], c3[k]);
         const int vs = d * ld;
         float* base = P.mx + ((side * 9) * d + kx) * ld + j;
+        // the next field's memory variables are loaded before this field's
+        // stores (which the compiler must assume could alias them)
+        float nm[3][Q];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) ldv(base + v * vs, nm[v]);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             float F0v[Q], Fav[Q], Fdv[Q];
@@ -405,9 +434,12 @@ __device__ __forceinline__ void cpml_vec(const PropDesc& P, const Stage& st, int
             ldv(&st.halo[f][c - 1][r0], Fdv);
             float* m = base + (f * 3) * vs;
             float m1[Q], m2[Q], m3[Q];
-            ldv(m, m1);
-            ldv(m + vs, m2);
-            ldv(m + 2 * vs, m3);
+#pragma unroll
+            for (int k = 0; k < Q; ++k) { m1[k] = nm[0][k]; m2[k] = nm[1][k]; m3[k] = nm[2][k]; }
+            if (f < 2) {
+#pragma unroll
+                for (int v = 0; v < 3; ++v) ldv(m + (3 + v) * vs, nm[v]);
+            }
 #pragma unroll
             for (int k = 0; k < Q; ++k) {
                 float F0 = F0v[k], Fa = Fav[k], Fd = Fdv[k];
@@ -444,6 +476,9 @@ __device__ __forceinline__ void cpml_vec(const PropDesc& P, const Stage& st, int
         }
         const int vs = nx * P.dpz;
         float* base = P.mz + ((side * 9) * nx + i) * P.dpz + k0;
+        float nm[3][Q];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) ldv(base + v * vs, nm[v]);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const float* col = &st.halo[f][c][r0];
@@ -453,9 +488,12 @@ __device__ __forceinline__ void cpml_vec(const PropDesc& P, const Stage& st, int
             Fc[Q + 1] = col[Q];
             float* m = base + (f * 3) * vs;
             float m1[Q], m2[Q], m3[Q];
-            ldv(m, m1);
-            ldv(m + vs, m2);
-            ldv(m + 2 * vs, m3);
+#pragma unroll
+            for (int k = 0; k < Q; ++k) { m1[k] = nm[0][k]; m2[k] = nm[1][k]; m3[k] = nm[2][k]; }
+            if (f < 2) {
+#pragma unroll
+                for (int v = 0; v < 3; ++v) ldv(m + (3 + v) * vs, nm[v]);
+            }
 #pragma unroll
             for (int k = 0; k < Q; ++k) {
                 float F0 = Fc[k + 1], Fa = Fc[k + 2], Fd = Fc[k];
@@ -642,6 +680,7 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
             // lean: every point of the group inside the image region (no CPML, no edge)
             const bool lean = i >= d && i < nx - d && j >= d && j + Q - 1 < nz - d;
             float2 s2u[2], s2v[2], s2w[2];
+            if (!lean && d > 0) prefetch_strip_state(P, j, i);
             {
                 Window win;            // dies here: later phases re-read the stage
                 win.load(st, c, r0);
