@@ -63,10 +63,14 @@ enum { MNAD_SNAP_F32 = 0, MNAD_SNAP_BF16 = 1, MNAD_SNAP_F16 = 2 };
 enum { MNAD_PAIR_REFERENCE = 0, MNAD_PAIR_ALIGNED = 1 };
 
 /* Step kernel choice.  AUTO picks per launch group (propagations of one grid
- * size advancing together): the persistent TMA kernel once a launch has about
- * 2.25 of its 64 x 16 tiles per resident CTA (0.7M point-updates on a
- * 152-SM GB300), the one-thread-per-point kernel below. */
-enum { MNAD_KERNEL_AUTO = 0, MNAD_KERNEL_DIRECT = 1, MNAD_KERNEL_TMA = 2 };
+ * size advancing together): the persistent TMA kernel (64 x 16 tiles) once a
+ * launch has about 2.25 of its tiles per resident CTA (0.7M point-updates on
+ * a 152-SM GB300), the one-thread-per-point kernel (32 x 8 tiles) below.
+ * TUNE measures both on each launch group of a plan or job batch at its first
+ * run (10 trial steps each, before the run starts from zero state) and keeps
+ * the faster; choices are cached in the context per grid, CPML width and
+ * propagation count.  The serving loop treats TUNE as AUTO. */
+enum { MNAD_KERNEL_AUTO = 0, MNAD_KERNEL_DIRECT = 1, MNAD_KERNEL_TMA = 2, MNAD_KERNEL_TUNE = 3 };
 
 typedef struct mnad_options {
     int snapshot_codec;   /* MNAD_SNAP_*; default MNAD_SNAP_F32 */

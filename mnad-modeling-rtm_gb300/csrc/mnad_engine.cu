@@ -570,14 +570,7 @@ void Batch::finalize()
         nsteps_ = std::max(nsteps_, p->spec.nt);
     }
     for (auto& g : groups_) {
-        // the group's step kernel: forced, or by the measured crossover
-        if (tc_.kind == MNAD_KERNEL_DIRECT || tc_.kind == MNAD_KERNEL_TMA) g->kind = tc_.kind;
-        else {
-            const double tiles = (double)g->props.size() * ((g->nz + TMA_TZ - 1) / TMA_TZ) *
-                                 ((g->nx + TMA_TX - 1) / TMA_TX);
-            g->kind = tiles >= AUTO_TMA_TILES_PER_CTA * ctx_.num_sms * TMA_CTAS_PER_SM ? MNAD_KERNEL_TMA
-                                                                                      : MNAD_KERNEL_DIRECT;
-        }
+        g->kind = pick_kind(*g);
         const bool tma = g->kind == MNAD_KERNEL_TMA;
         g->ntz = tma ? (g->nz + TMA_TZ - 1) / TMA_TZ : (g->nz + DIRECT_TZ - 1) / DIRECT_TZ;
         g->tiles_per_prop = g->ntz * (tma ? (g->nx + TMA_TX - 1) / TMA_TX : (g->nx + DIRECT_TX - 1) / DIRECT_TX);
@@ -633,11 +626,86 @@ void Batch::finalize()
     upload(ctx_, d_all_desc_.get(), all.data(), all.size() * sizeof(PropDesc));
 }
 
+// The group's step kernel: forced, a tuning trial, a measured choice, or the
+// crossover rule.
+int Batch::pick_kind(const LaunchGroup& g) const
+{
+    if (tc_.kind == MNAD_KERNEL_DIRECT || tc_.kind == MNAD_KERNEL_TMA) return tc_.kind;
+    if (tc_.kind == MNAD_KERNEL_TUNE) {
+        if (trial_kind_ >= 0) return trial_kind_;
+        auto it = ctx_.kernel_choice.find(std::make_tuple(g.nz, g.nx, g.d, (int)g.props.size()));
+        if (it != ctx_.kernel_choice.end()) return it->second;
+    }
+    const double tiles = (double)g.props.size() * ((g.nz + TMA_TZ - 1) / TMA_TZ) * ((g.nx + TMA_TX - 1) / TMA_TX);
+    return tiles >= AUTO_TMA_TILES_PER_CTA * ctx_.num_sms * TMA_CTAS_PER_SM ? MNAD_KERNEL_TMA : MNAD_KERNEL_DIRECT;
+}
+
+void Batch::tune()
+{
+    if (tc_.kind != MNAD_KERNEL_TUNE || tuned_) return;
+    tuned_ = true;
+    const int K = std::min(TUNE_STEPS, nsteps_ - TUNE_WARMUP);
+    bool known = true;
+    for (const auto& g : groups_)
+        known &= ctx_.kernel_choice.count(std::make_tuple(g->nz, g->nx, g->d, (int)g->props.size())) > 0;
+    if (known || K < 2 || ntiles_ == 0) return;     // cached, or too short to measure: the rule stands
+    const int ng = (int)groups_.size();
+    const int kinds[2] = {MNAD_KERNEL_DIRECT, MNAD_KERNEL_TMA};
+    std::vector<double> ms[2];
+    std::vector<cudaEvent_t> ev((size_t)2 * K * ng, nullptr);
+    for (auto& e : ev) MNAD_CK(cudaEventCreate(&e));
+    try {
+        for (int c = 0; c < 2; ++c) {
+            trial_kind_ = kinds[c];
+            finalize();
+            start();
+            const int n = TUNE_WARMUP + K;
+            if (has_tma()) {
+                const size_t need = reserve_counters(n);
+                MNAD_CK(cudaMemsetAsync(d_counters_.get(), 0, need, ctx_.stream));
+            }
+            for (int s = 0; s < n; ++s)
+                for (int gi = 0; gi < ng; ++gi) {
+                    const int t = s - TUNE_WARMUP;
+                    if (t >= 0) MNAD_CK(cudaEventRecord(ev[(size_t)2 * (t * ng + gi)], ctx_.stream));
+                    launch_group(gi, s, s);
+                    if (t >= 0) MNAD_CK(cudaEventRecord(ev[(size_t)2 * (t * ng + gi) + 1], ctx_.stream));
+                }
+            MNAD_CK(cudaGetLastError());
+            MNAD_CK(cudaStreamSynchronize(ctx_.stream));
+            ms[c].assign(ng, 0.0);
+            for (int t = 0; t < K; ++t)
+                for (int gi = 0; gi < ng; ++gi) {
+                    float x = 0;
+                    MNAD_CK(cudaEventElapsedTime(&x, ev[(size_t)2 * (t * ng + gi)], ev[(size_t)2 * (t * ng + gi) + 1]));
+                    ms[c][gi] += x;
+                }
+        }
+    } catch (...) {
+        for (auto& e : ev) cudaEventDestroy(e);
+        trial_kind_ = -1;
+        throw;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    for (int gi = 0; gi < ng; ++gi) {
+        const LaunchGroup& g = *groups_[gi];
+        ctx_.kernel_choice[std::make_tuple(g.nz, g.nx, g.d, (int)g.props.size())] =
+            ms[0][gi] <= ms[1][gi] ? MNAD_KERNEL_DIRECT : MNAD_KERNEL_TMA;
+    }
+    trial_kind_ = -1;
+    finalize();
+}
+
 void Batch::launch_step(int s, int slot)
 {
-    for (size_t gi = 0; gi < groups_.size(); ++gi) {
+    for (size_t gi = 0; gi < groups_.size(); ++gi) launch_group(gi, s, slot);
+}
+
+void Batch::launch_group(size_t gi, int s, int slot)
+{
+    {
         auto& g = groups_[gi];
-        if (g->ntiles == 0) continue;
+        if (g->ntiles == 0) return;
         StepArgs a;
         a.coef = g->coefs;
         for (int k = 0; k < NCOEF; ++k) {
@@ -812,6 +880,13 @@ void Batch::tick(int K, bool use_graph)
 void Batch::run(bool use_graph)
 {
     if (ntiles_ == 0) return;
+    if (tc_.kind == MNAD_KERNEL_TUNE && !tuned_) {
+        tune();
+        if (graph_) {                      // captured with the kernels of the rule
+            cudaGraphExecDestroy(graph_);
+            graph_ = nullptr;
+        }
+    }
     auto body = [&]() {
         start();
         advance(0, nsteps_);

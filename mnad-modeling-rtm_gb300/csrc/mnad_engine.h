@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -66,6 +67,8 @@ struct Context {
     int num_sms = 0;
     unsigned* d_status = nullptr;
     std::map<int, std::unique_ptr<Wavefield>> wavefields;
+    // MNAD_KERNEL_TUNE: measured step kernel per (nz, nx, d_pml, propagations per launch)
+    std::map<std::tuple<int, int, int, int>, int> kernel_choice;
     std::vector<double> last_energy;  // energy history of the last drop-in forward
 
     explicit Context(int dev, size_t budget_bytes);
@@ -76,10 +79,11 @@ struct Context {
     unsigned take_status();
 };
 
-// Step-kernel choice of a batch: MNAD_KERNEL_DIRECT, MNAD_KERNEL_TMA, or
+// Step-kernel choice of a batch: MNAD_KERNEL_DIRECT, MNAD_KERNEL_TMA,
 // MNAD_KERNEL_AUTO (per launch group: the TMA kernel once a launch has
 // AUTO_TMA_TILES_PER_CTA of its tiles for each resident CTA, the direct
-// kernel below).
+// kernel below) or MNAD_KERNEL_TUNE (per launch group, measured on the
+// batch's own propagations at its first run; Batch::tune).
 struct TileCfg {
     int kind;
     int tz, tx;   // receiver bucket tile: TMA_TZ x TMA_TX for every kernel
@@ -91,6 +95,7 @@ TileCfg tile_cfg(int kernel);
 // the persistent TMA kernel from 0.82M (800 tiles, 2.6 per CTA) on; its
 // pipeline needs a few tiles per CTA to hide the load latency.
 constexpr double AUTO_TMA_TILES_PER_CTA = 2.25;
+constexpr int TUNE_WARMUP = 2, TUNE_STEPS = 8;
 
 // Receivers of one propagation bucketed by TMA_TZ x TMA_TX tile and, within a
 // tile, by column (stable counting sort): entries of tile t are
@@ -174,6 +179,11 @@ public:
     void add(Prop* p) { props_.push_back(p); }
     void finalize();
     void run(bool use_graph);          // start() + every step, optionally as one CUDA graph (async)
+    // MNAD_KERNEL_TUNE: time TUNE_STEPS steps of every launch group with
+    // each step kernel (after TUNE_WARMUP untimed ones) and keep the faster
+    // per group; choices are cached in the context.  The trial steps leave
+    // no trace: run() starts from start(), which resets what they touched.
+    void tune();
     void start();                      // zero all state and seed the sources (async)
     void advance(int s0, int s1);      // launch global steps s0..s1-1 (async)
     void refresh_descs();              // re-upload the descriptors after host-side changes
@@ -191,12 +201,16 @@ public:
     const std::vector<Prop*>& props() const { return props_; }
 private:
     void launch_step(int s, int slot);
+    void launch_group(size_t gi, int s, int slot);
+    int pick_kind(const LaunchGroup& g) const;
     size_t reserve_counters(int nsteps);   // tile counters for nsteps steps (bytes used)
     void encode_snapshots(int s);      // FP16 codec: encode the snapshots taken at step s
     void energy_after(int s);          // energy diagnostic after step s
     void checkpoint_after(int s);      // checkpointed propagations: save the state after step s
     Context& ctx_;
     TileCfg tc_;
+    int trial_kind_ = -1;              // tune(): kernel forced on every group during a trial
+    bool tuned_ = false;
     std::vector<Prop*> props_;
     std::vector<std::unique_ptr<LaunchGroup>> groups_;
     DevMem d_all_desc_;                // every descriptor (source seeding)

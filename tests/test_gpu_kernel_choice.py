@@ -1,4 +1,5 @@
-"""GPU tests of the per-launch-group step-kernel choice (MNAD_KERNEL_AUTO).
+"""GPU tests of the per-launch-group step-kernel choice (MNAD_KERNEL_AUTO,
+and the measured choice MNAD_KERNEL_TUNE).
 
 A plan whose propagations fall into a small launch group (fewer than 2.25
 TMA tiles of 64 x 16 points per resident CTA: the direct kernel) and a large
@@ -42,9 +43,13 @@ def _jobs(nz, nx, n, nt, seed, d=10):
     return out
 
 
+def _copies(jobs):
+    return [mnad.ShotJob(kind=j.kind, v=j.v, dx=j.dx, dz=j.dz, dt=j.dt, nt=j.nt, d_pml=j.d_pml, zs=j.zs, xs=j.xs,
+                         zr=j.zr, xr=j.xr, w=j.w) for j in jobs]
+
+
 def _run(kernel, small, large):
-    jobs = [mnad.ShotJob(kind=j.kind, v=j.v, dx=j.dx, dz=j.dz, dt=j.dt, nt=j.nt, d_pml=j.d_pml, zs=j.zs, xs=j.xs,
-                         zr=j.zr, xr=j.xr, w=j.w) for j in small + large]
+    jobs = _copies(small + large)
     with mnad.Context(0, kernel=kernel) as ctx:
         ctx.run_jobs(jobs)
         assert ctx.status() == 0
@@ -68,3 +73,27 @@ def test_auto_picks_the_kernel_per_launch_group():
         ref = coracle.fwd(j.dx, int(j.xs), j.xr, j.dz, int(j.zs), j.zr, j.v, j.dt, j.nt, j.w, j.d_pml)["datau"]
         assert rel(direct[k], ref) <= TOL_GATHER
         assert rel(tma[k], ref) <= TOL_GATHER
+
+
+def test_tuned_choice_matches_a_forced_kernel_and_is_cached():
+    """TUNE runs trial steps of both kernels before the real run; the outputs
+    of each group are bitwise those of one forced kernel (the trial leaves no
+    trace), and a second batch of the same shape in the context reuses the
+    cached choice with the same outputs."""
+    small = _jobs(96, 112, 3, 160, 1)
+    large = _jobs(360, 376, 8, 160, 2)
+    ns = len(small)
+    direct = _run("direct", small, large)
+    tma = _run("tma", small, large)
+    with mnad.Context(0, kernel="tune") as ctx:
+        first = _copies(small + large)
+        ctx.run_jobs(first)
+        again = _copies(small + large)
+        ctx.run_jobs(again)
+        assert ctx.status() == 0
+    for group in (range(ns), range(ns, len(first))):
+        ks = list(group)
+        same_direct = all(np.array_equal(first[k].data, direct[k]) for k in ks)
+        same_tma = all(np.array_equal(first[k].data, tma[k]) for k in ks)
+        assert same_direct or same_tma
+        assert all(np.array_equal(first[k].data, again[k].data) for k in ks)
