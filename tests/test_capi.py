@@ -83,3 +83,32 @@ def test_options_struct_matches_header():
                         body)
     flat = [x for tup in fields for x in tup if x]
     assert flat == [f for f, _ in _lib.Job._fields_]
+
+
+def test_enum_constants_match_header():
+    """Every MNAD_* enumerator of the header has the same value in the
+    Python binding (status codes, codecs, pairings, kernels, job kinds and
+    states)."""
+    src = open(HEADER).read()
+    header = {}
+    for body in re.findall(r"enum\s*\{(.*?)\}", src, re.S):
+        body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+        for name, val in re.findall(r"MNAD_(\w+)\s*=\s*(\d+)", body):
+            header[name] = int(val)
+    assert len(header) >= 24
+    for name, val in header.items():
+        assert getattr(_lib, name) == val, name
+
+
+def test_server_structs_match_header():
+    src = open(HEADER).read()
+    body = re.search(r"typedef struct mnad_server_options \{(.*?)\} mnad_server_options;", src, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"(?:size_t|int)\s+(\w+);", body)
+    assert fields == [f for f, _ in _lib.ServerOptions._fields_]
+    body = re.search(r"typedef struct mnad_server_stats \{(.*?)\} mnad_server_stats;", src, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for decl in re.findall(r"(?:int64_t|double|size_t)\s+([\w\s,]+);", body):
+        fields += [f.strip() for f in decl.split(",")]
+    assert fields == [f for f, _ in _lib.ServerStats._fields_]
