@@ -48,15 +48,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config3", choices=["config3", "config5"],
-                    help="config3: batched RTM (default); config5: large-grid RTM with FP16 checkpoints")
-    ap.add_argument("--shots", type=int, default=None, help="shots per pass (config3: 64, config5: 16)")
-    ap.add_argument("--nt", type=int, default=None, help="record length in steps (config3: 4000, config5: 6000)")
-    ap.add_argument("--checkpoint-every", type=int, default=360, help="config5: checkpoint interval (steps)")
+    ap.add_argument("--workload", default="random-field", choices=["random-field", "faulted-salt"],
+                    help="random-field: batched RTM of 64 shots over a 401x1201 Gaussian random field (default); "
+                         "faulted-salt: RTM of 16 shots over a 1201x4001 faulted model with FP16 checkpoints")
+    ap.add_argument("--shots", type=int, default=None, help="shots per pass (random-field: 64, faulted-salt: 16)")
+    ap.add_argument("--nt", type=int, default=None,
+                    help="record length in steps (random-field: 4000, faulted-salt: 6000)")
+    ap.add_argument("--checkpoint-every", type=int, default=360, help="faulted-salt: checkpoint interval (steps)")
     ap.add_argument("--plain-shots", type=int, default=2)
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, plain and CPU legs")
     ap.add_argument("--ref-steps", type=int, default=12, help="reference arm: time steps per worker sample")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "direct", "tma"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "direct", "tma", "tune"])
     ap.add_argument("--serve-jobs", type=int, default=512, help="served stream length (0: skip the leg)")
     ap.add_argument("--serve-rate", type=float, default=None, help="arrivals per second (default: from the seed)")
     return ap.parse_args()
@@ -221,7 +223,7 @@ def serving_leg(device, njobs, rate=None, seed=0, kernel="auto"):
     import numpy as np
     import mnad
     from mnad import workflow
-    sched, pools, rate = workflow.config4(seed=seed, njobs=njobs, rate=rate)
+    sched, pools, rate = workflow.served_stream(seed=seed, njobs=njobs, rate=rate)
     # warm-up server (module load, first allocations of the memory pool)
     with mnad.Server(device, kernel=kernel) as w:
         for sj in sched[:4]:
@@ -266,7 +268,7 @@ def serving_leg(device, njobs, rate=None, seed=0, kernel="auto"):
     srv.close()
     if err:
         raise err[0]
-    return {"workload": "served shot stream, config 4", "jobs": len(sched), "model_jobs": kinds["model"],
+    return {"workload": "served shot stream of mixed modeling / RTM jobs on 256x256 to 1024x2048 grids", "jobs": len(sched), "model_jobs": kinds["model"],
             "rtm_jobs": kinds["rtm"], "arrival_rate_per_s": round(rate, 3),
             "grids": [f"{g[0]}x{g[1]}" for g in workflow.SERVED_GRIDS], "seconds": list(workflow.SERVED_SECONDS),
             "value": round(st["point_updates"] / wall / 1e9, 3), "unit": "Gpts/s",
@@ -282,20 +284,20 @@ def run_ours(args):
     rank, world, local = dist_setup(args.gpus)
     import mnad
     from mnad import shards, workflow
-    if args.workload == "config5":
-        sv = workflow.config5(seed=0, nshots=256, nt=args.nt, first=rank * args.shots, count=args.shots)
+    if args.workload == "faulted-salt":
+        sv = workflow.faulted_salt_survey(seed=0, nshots=256, nt=args.nt, first=rank * args.shots, count=args.shots)
         ctx = mnad.Context(local, kernel=args.kernel, checkpoint_every=args.checkpoint_every, checkpoint_codec="f16")
         data_desc = "synthetic (seeded faulted layered model with a salt body)"
-        wl = {"workload": "large-grid RTM with checkpoint-and-recompute, config 5",
+        wl = {"workload": "large-grid RTM with checkpoint-and-recompute, 1201x4001 faulted model with a salt body",
               "grid": "1201x4001 (+2x40 CPML) @ 12.5 m", "checkpoints": f"f16 every {args.checkpoint_every} steps",
               "snapshot_buffer": "f32 segment", "propagations_per_shot": "3 + 1 recomputed background forward"}
     else:
         # weak scaling: every rank images args.shots shots of one survey
-        sv = workflow.config3(seed=0, nshots=args.shots * world, nt=args.nt)
+        sv = workflow.random_field_survey(seed=0, nshots=args.shots * world, nt=args.nt)
         sv.shots = shards.shard(sv.shots, rank, world)
         ctx = mnad.Context(local, snapshot_codec=sv.codec, kernel=args.kernel)
         data_desc = "synthetic (seeded Gaussian random field + dipping reflectors)"
-        wl = {"workload": "batched RTM, config 3", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
+        wl = {"workload": "batched RTM of 64 shots, 401x1201 Gaussian random field with dipping reflectors", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
               "snapshots": sv.codec, "propagations_per_shot": 3}
     jobs = workflow.shot_jobs(sv, "rtm")
     m0 = ctx.memory()
@@ -333,7 +335,7 @@ def run_ours(args):
     achieved = abytes * args.steps / (sum(step_ms) / 1e3) / 1e9
     tr = profile_traffic()
     traffic = None
-    if tr and "bytes_per_point_update" in tr and args.workload == "config3":
+    if tr and "bytes_per_point_update" in tr and args.workload == "random-field":
         traffic = tr["bytes_per_point_update"] * pts / (plan.timing()["step_launches"])
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -396,7 +398,7 @@ def run_ours(args):
         if rank == 0:
             extras["cpu_baseline"] = cpu_baseline(sv)
     ctx.close()
-    if rank == 0 and args.serve_jobs > 0 and not args.no_extras and args.workload == "config3":
+    if rank == 0 and args.serve_jobs > 0 and not args.no_extras and args.workload == "random-field":
         extras["serving"] = serving_leg(local, args.serve_jobs, args.serve_rate, kernel=args.kernel)
         # the same stream all at once: the server's capacity (latency is then queueing)
         cap = serving_leg(local, args.serve_jobs, 1e6, kernel=args.kernel)
@@ -429,7 +431,7 @@ _REF = {}
 def _ref_init(seed, nshots, nt):
     from mnad import workflow
     from oracle import mnad_oracle as P
-    sv = workflow.config3(seed=seed, nshots=nshots, nt=nt)
+    sv = workflow.random_field_survey(seed=seed, nshots=nshots, nt=nt)
     _REF["sv"] = sv
     _REF["A"] = P.a_gen(sv.dx, sv.dz, sv.dt, sv.v)
 
@@ -465,13 +467,13 @@ def run_reference(args):
             vals.append(sum(r[1] for r in res) / el / 1e9)
         wall = time.perf_counter() - t0
     value = statistics.median(vals)
-    sample = (f"{workers} worker processes (parfor analogue), each one shot of config 3 for {args.ref_steps} "
+    sample = (f"{workers} worker processes (parfor analogue), each one shot of the 401x1201 random-field survey for {args.ref_steps} "
               f"time steps (401x1201 + 2x40 CPML), literal FP64 sparse-operator restatement (SciPy)")
     line = {"metric": METRIC, "value": round(value, 5), "unit": "Gpts/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(wall * 1e3 / args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Gaussian random field + dipping reflectors)",
-            "config": {"workload": "batched RTM, config 3", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
+            "config": {"workload": "batched RTM of 64 shots, 401x1201 Gaussian random field with dipping reflectors", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
                        "shots": args.shots, "nt": args.nt, "parallelism": f"{workers} host processes"},
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 5), "unit": "Gpts/s", "cores": workers, "kind": "port",
@@ -483,9 +485,9 @@ def run_reference(args):
 if __name__ == "__main__":
     a = parse()
     if a.shots is None:
-        a.shots = 16 if a.workload == "config5" else 64
+        a.shots = 16 if a.workload == "faulted-salt" else 64
     if a.nt is None:
-        a.nt = 6000 if a.workload == "config5" else 4000
+        a.nt = 6000 if a.workload == "faulted-salt" else 4000
     if a.impl == "reference":
         run_reference(a)
     else:

@@ -84,17 +84,17 @@ class Survey:
         return self.v.shape[1]
 
 
-def config1(nt: int = 1000) -> Survey:
+def constant_velocity_shot(nt: int = 1000) -> Survey:
     """Plain FP64 forward modeling: 201 x 201 total grid (physical 161 x 161
     plus a 20-point CPML), 10 m, 2000 m/s, 20 Hz Ricker at (101,101),
     dt = 1 ms, 201 receivers on row 21 (the first physical row)."""
     d = 20
     v = np.full((201, 201), 2000.0)
     shot = Shot(101, 101, np.full(201, 21), np.arange(1, 202))
-    return Survey("config1", v, 10.0, 10.0, 1e-3, nt, d, 20.0, [shot])
+    return Survey("constant velocity 201x201", v, 10.0, 10.0, 1e-3, nt, d, 20.0, [shot])
 
 
-def config2(seed: int = 0, nt: int = 3000, T: int = 4) -> Survey:
+def layered_anomaly_shot(seed: int = 0, nt: int = 3000, T: int = 4) -> Survey:
     """Single-shot RTM: 301 (z) x 601 (x) at 10 m, layers 1500/2000/2600/3200
     m/s with interfaces at 800/1600/2400 m, +300 m/s Gaussian anomaly
     (sigma 150 m, centre from the seed); migration model = true model
@@ -112,7 +112,7 @@ def config2(seed: int = 0, nt: int = 3000, T: int = 4) -> Survey:
     Vs = gaussian_smooth(V, 15)
     xs_grid, zs_grid, zr_grid = 300, 1, 2
     shot = Shot(d + zs_grid, d + xs_grid, np.full(nxp, d + zr_grid), d + np.arange(1, nxp + 1))
-    return Survey("config2", pad_model(V, d), h, h, 1e-3, nt, d, 15.0, [shot], vs=pad_model(Vs, d), T=T,
+    return Survey("layered + anomaly 301x601", pad_model(V, d), h, h, 1e-3, nt, d, 15.0, [shot], vs=pad_model(Vs, d), T=T,
                   meta={"anomaly_centre_m": (cz, cx)})
 
 
@@ -126,7 +126,7 @@ def gaussian_random_field(shape, h, corr, rng):
     return (f - f.mean()) / (f.std() + 1e-30)
 
 
-def config3(seed: int = 0, nshots: int = 64, nt: int = 4000, codec: str = "bf16") -> Survey:
+def random_field_survey(seed: int = 0, nshots: int = 64, nt: int = 4000, codec: str = "bf16") -> Survey:
     """Batched RTM: 401 (z) x 1201 (x) at 12.5 m; smooth Gaussian random field
     (correlation 300 m) clipped to 1500-4000 m/s plus three dipping
     +400 m/s reflectors; ``nshots`` shots every 187.5 m; 20 Hz; dt = 1 ms;
@@ -151,7 +151,7 @@ def config3(seed: int = 0, nshots: int = 64, nt: int = 4000, codec: str = "bf16"
     for s in range(nshots):
         xg = max(1, min(nxp, first + s * spacing))
         shots.append(Shot(d + 1, d + xg, np.full(nxp, d + 2), d + np.arange(1, nxp + 1)))
-    return Survey("config3", pad_model(V, d), h, h, 1e-3, nt, d, 20.0, shots, vs=pad_model(Vs, d), codec=codec)
+    return Survey("random field 401x1201", pad_model(V, d), h, h, 1e-3, nt, d, 20.0, shots, vs=pad_model(Vs, d), codec=codec)
 
 
 def faulted_model(nz: int, nx: int, h: float, rng, nfaults: int = 6) -> np.ndarray:
@@ -186,7 +186,7 @@ def faulted_model(nz: int, nx: int, h: float, rng, nfaults: int = 6) -> np.ndarr
     return np.clip(V, 1500.0, 4500.0)
 
 
-def config5(seed: int = 0, nshots: int = 256, nt: int = 6000, first: int = 0, count: Optional[int] = None) -> Survey:
+def faulted_salt_survey(seed: int = 0, nshots: int = 256, nt: int = 6000, first: int = 0, count: Optional[int] = None) -> Survey:
     """Large-scale RTM at 2 points per minimum wavelength: 1201 (z) x 4001 (x)
     at 12.5 m (1281 x 4081 padded), vmin 1500 m/s; seeded faulted
     sedimentary model with a 4500 m/s salt body; ``nshots`` shots spread over
@@ -203,7 +203,7 @@ def config5(seed: int = 0, nshots: int = 256, nt: int = 6000, first: int = 0, co
     for s in range(first, first + count):
         xg = int(round(step * (s + 0.5))) + 1
         shots.append(Shot(d + 1, d + xg, np.full(nxp, d + 2), d + np.arange(1, nxp + 1)))
-    return Survey("config5", pad_model(V, d), h, h, 1e-3, nt, d, 25.0, shots, vs=pad_model(Vs, d), codec="f32",
+    return Survey("faulted + salt 1201x4001", pad_model(V, d), h, h, 1e-3, nt, d, 25.0, shots, vs=pad_model(Vs, d), codec="f32",
                   meta={"nshots_total": nshots})
 
 
@@ -256,7 +256,7 @@ class ServedJob:
     xs: int           # 1-based padded source column
 
 
-def config4(seed: int = 0, njobs: int = 512, rate: Optional[float] = None, models_per_grid: int = 4,
+def served_stream(seed: int = 0, njobs: int = 512, rate: Optional[float] = None, models_per_grid: int = 4,
             d_pml: int = 20):
     """Served shot stream: Poisson arrivals of ``njobs`` jobs, 70 % modeling
     and 30 % RTM, grids drawn uniformly from SERVED_GRIDS at 10 m, record

@@ -11,7 +11,7 @@ and stores their outputs:
   floor(nt/T) < 2nf+1 (the reference's pairing shifted by one snapshot),
   nt = 247 (aligned) and nt = 239, where floor(nt/T) > 2nf+1 and UU grows
   past its preallocated columns;
-* golden_ref_config1.npz: config 1 (201 x 201, 20-point CPML, 2000 m/s,
+* golden_ref_constant_velocity.npz: the constant-velocity shot (201 x 201, 20-point CPML, 2000 m/s,
   20 Hz Ricker at the centre, 201 receivers on row 21, nt = 1000), the
   reference's own CPU case;
 * golden_ref_prep.npz: SRC/MNAD/acquisi.m for the 'fixspread', 'onesided',
@@ -86,7 +86,7 @@ def rtm_case(it, nt, seed=0):
                 xs=xs, data=data, datas=datas, UU=UU, illum=illum, Im=Im.ravel())
 
 
-def config1_case(it):
+def constant_velocity_case(it):
     nz = nx = 201
     d, nt, dt, dx = 20, 1000, 1e-3, 10.0
     v = np.full((nz, nx), 2000.0)
@@ -132,11 +132,11 @@ def main():
     out = {f"{n}_{k}": val for n, case in cases.items() for k, val in case.items()}
     np.savez_compressed(os.path.join(HERE, "golden_ref_rtm.npz"), **out)
     np.savez_compressed(os.path.join(HERE, "golden_ref_prep.npz"), **prep_case(it))
-    c = config1_case(it)
-    np.savez_compressed(os.path.join(HERE, "golden_ref_config1.npz"), **c)
+    c = constant_velocity_case(it)
+    np.savez_compressed(os.path.join(HERE, "golden_ref_constant_velocity.npz"), **c)
     for name, case in cases.items():
         print(name, "nt", case["nt"], "UU", case["UU"].shape, "|Im|", np.linalg.norm(case["Im"]))
-    print("config1 |data|", np.linalg.norm(c["data"]))
+    print("constant velocity |data|", np.linalg.norm(c["data"]))
 
 
 if __name__ == "__main__":

@@ -1,9 +1,10 @@
 """Full-size parity of the benchmark configurations against the FP64 C
-oracle: config 2 (single-shot RTM, 381 x 681 padded, 3 s, T = 4), one
-shot of config 3 (481 x 1281 padded, 4 s, snapshot interval by the reference
-formula) with FP32 and BF16 snapshots, and one checkpointed shot on config 5's
-1281 x 4081 grid (1 s) with FP32 and FP16 checkpoints; at config 5's full 6 s
-the checkpointed runs are checked against the stored-snapshot run.  Each error is printed so the run log
+oracle: the layered single-shot RTM (381 x 681 padded, 3 s, T = 4), one
+shot of the 64-shot random-field survey (481 x 1281 padded, 4 s, snapshot
+interval by the reference formula) with FP32 and BF16 snapshots, and one
+checkpointed shot on the faulted-salt survey's 1281 x 4081 grid (1 s) with FP32
+and FP16 checkpoints; at that survey's full 6 s the checkpointed runs are
+checked against the stored-snapshot run.  Each error is printed so the run log
 states it for every gather, snapshot set and image."""
 import numpy as np
 import pytest
@@ -68,23 +69,23 @@ def _check(name, ctx, sv, shot, codecs):
 
 
 @pytest.mark.parametrize("kernel", ["direct", "tma"])
-def test_config2_full_size(ctx, kernel):
+def test_layered_single_shot_full_size(ctx, kernel):
     """381 - 40 is not a multiple of 4: the bottom CPML strip's storage rows
     start one row above the strip, which the damping profile must not see."""
-    sv = workflow.config2()
+    sv = workflow.layered_anomaly_shot()
     ctx.set_options(kernel=kernel)
     try:
-        _check(f"config2 {kernel}", ctx, sv, sv.shots[0], ("f32", "bf16"))
+        _check(f"layered 381x681 {kernel}", ctx, sv, sv.shots[0], ("f32", "bf16"))
     finally:
         ctx.set_options(kernel="auto")
 
 
-def test_config3_one_shot_full_size(ctx):
-    sv = workflow.config3(nshots=64)
-    _check("config3 shot 32", ctx, sv, sv.shots[32], ("f32", "bf16"))
+def test_random_field_shot_full_size(ctx):
+    sv = workflow.random_field_survey(nshots=64)
+    _check("random field 481x1281 shot 32", ctx, sv, sv.shots[32], ("f32", "bf16"))
 
 
-def _config5_plan(sv, **opts):
+def _faulted_plan(sv, **opts):
     jobs = workflow.shot_jobs(sv, "rtm", keep_data=True)
     with mnad.Context(0, **opts) as c:
         plan = c.plan(jobs)
@@ -95,38 +96,38 @@ def _config5_plan(sv, **opts):
     return jobs[0]
 
 
-def test_config5_checkpointed_shot_against_the_oracle():
-    """Config 5's full 1281 x 4081 grid, shot 222 of 256 (its first reflector
+def test_faulted_salt_checkpointed_shot_against_the_oracle():
+    """The faulted-salt survey's full 1281 x 4081 grid, shot 222 of 256 (its first reflector
     is the shallowest of the line, 600 m), cut to 1 s so that the FP64
     oracle's three propagations take about a minute (T = 9 by the reference
     formula).  The adjoint runs in segments from checkpoints every 360 steps,
     FP32 and FP16 codecs."""
-    sv = workflow.config5(nshots=256, nt=1000, first=222, count=1)
+    sv = workflow.faulted_salt_survey(nshots=256, nt=1000, first=222, count=1)
     sh = sv.shots[0]
     data, bg, im_ref, T = _oracle_rtm(sv, sh, sv.T)
     sct = data - bg["datau"]
     for codec, tol in (("f32", TOL_IMAGE), ("f16", TOL_F16)):
-        j = _config5_plan(sv, checkpoint_every=360, checkpoint_codec=codec)
+        j = _faulted_plan(sv, checkpoint_every=360, checkpoint_codec=codec)
         errs = dict(scattered=rel(j.data, sct), illum=rel(j.illum, bg["illum"]), image=rel(j.image, im_ref))
-        print(f"config5 shot 222, nt 1000, T={T}, {codec} checkpoints: " +
+        print(f"faulted salt shot 222, nt 1000, T={T}, {codec} checkpoints: " +
               ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
         assert errs["scattered"] <= 10 * TOL_GATHER
         assert errs["illum"] <= TOL_IMAGE
         assert errs["image"] <= tol
 
 
-def test_config5_full_length_checkpoints_match_stored_snapshots():
-    """One config-5 shot at its full 6 s: FP32 checkpoints replay the stored-
+def test_faulted_salt_full_length_checkpoints_match_stored_snapshots():
+    """One faulted-salt shot at its full 6 s: FP32 checkpoints replay the stored-
     snapshot run bitwise (image, illumination, scattered data); FP16
     checkpoints stay within the FP16 bar of it."""
-    sv = workflow.config5(nshots=256, first=128, count=1)
-    stored = _config5_plan(sv)
-    ck32 = _config5_plan(sv, checkpoint_every=360)
-    ck16 = _config5_plan(sv, checkpoint_every=360, checkpoint_codec="f16")
+    sv = workflow.faulted_salt_survey(nshots=256, first=128, count=1)
+    stored = _faulted_plan(sv)
+    ck32 = _faulted_plan(sv, checkpoint_every=360)
+    ck16 = _faulted_plan(sv, checkpoint_every=360, checkpoint_codec="f16")
     assert np.linalg.norm(stored.image) > 0
     assert np.array_equal(ck32.image, stored.image)
     assert np.array_equal(ck32.illum, stored.illum)
     assert np.array_equal(ck32.data, stored.data)
     e16 = rel(ck16.image, stored.image)
-    print(f"config5 shot 128, 6 s: FP16 checkpoints vs stored FP32 snapshots, image {e16:.2e}")
+    print(f"faulted salt shot 128, 6 s: FP16 checkpoints vs stored FP32 snapshots, image {e16:.2e}")
     assert e16 <= TOL_F16

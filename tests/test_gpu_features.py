@@ -120,7 +120,7 @@ def _energy_oracle(sv, sh, steps, every):
 
 
 def test_energy_diagnostic_matches_oracle_and_is_absorbed(ctx):
-    sv = workflow.config1(nt=700)
+    sv = workflow.constant_velocity_shot(nt=700)
     sh = sv.shots[0]
     every = 50
     ctx.set_options(energy_every=every)

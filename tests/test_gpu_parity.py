@@ -125,10 +125,10 @@ def test_misaligned_snapshot_pairing(ctx, pairing):
     ctx.wavefield_release(9)
 
 
-def test_config1_gather_and_snapshots(ctx):
-    """Config 1: 201x201, 2000 m/s, 20 Hz, nt=1000; gather and the wavefield
+def test_constant_velocity_gather_and_snapshots(ctx):
+    """Constant-velocity shot: 201x201, 2000 m/s, 20 Hz, nt=1000; gather and the wavefield
     at t = 0.3 s and 0.6 s (steps 300 and 600) against the FP64 oracle."""
-    sv = workflow.config1()
+    sv = workflow.constant_velocity_shot()
     sh = sv.shots[0]
     args = (sv.dx, sh.xs, sh.xr, sv.dz, sh.zs, sh.zr, sv.v, sv.dt, sv.nt, sv.w, sv.d_pml)
     datau, fields = ctx.fwd_fields(*args, steps=[300, 600])

@@ -1,7 +1,7 @@
 """GPU results against fixtures produced by the reference's own MATLAB
 sources (run under oracle/mlite.py; see tests/golden/make_reference_golden.py):
 three RTM record lengths covering the shifted, aligned and grown snapshot
-pairing of Born_adj_MNAD.m, and config 1's gather."""
+pairing of Born_adj_MNAD.m, and the constant-velocity 201 x 201 shot's gather."""
 import os
 
 import numpy as np
@@ -47,8 +47,8 @@ def test_rtm_shot_matches_the_reference_run(ctx, name):
     assert errs["image"] <= TOL_IMAGE
 
 
-def test_config1_gather_matches_the_reference_run(ctx):
-    g = np.load(os.path.join(GOLDEN, "golden_ref_config1.npz"))
+def test_constant_velocity_gather_matches_the_reference_run(ctx):
+    g = np.load(os.path.join(GOLDEN, "golden_ref_constant_velocity.npz"))
     nz, nx, nt, d = int(g["nz"]), int(g["nx"]), int(g["nt"]), int(g["d"])
     dt, dx, fc = float(g["dt"]), float(g["dx"]), float(g["fc"])
     t = np.arange(nt) * dt
@@ -58,5 +58,5 @@ def test_config1_gather_matches_the_reference_run(ctx):
     zr = np.full(xr.size, float(g["zr"]))
     out = ctx.fwd(dx, float(g["xs"]), xr, dx, float(g["zs"]), zr, np.full((nz, nx), float(g["v0"])), dt, nt, w, d)
     e = rel(out, g["data"])
-    print(f"config1 gather vs reference run: {e:.2e}")
+    print(f"constant-velocity gather vs reference run: {e:.2e}")
     assert e <= TOL_GATHER

@@ -63,8 +63,8 @@ def test_scipy_oracle_reproduces_the_reference_rtm_shot(ref):
     assert rel(im, c["Im"]) <= TOL
 
 
-def test_c_oracle_reproduces_the_reference_config1_gather():
-    g = np.load(os.path.join(GOLDEN, "golden_ref_config1.npz"))
+def test_c_oracle_reproduces_the_reference_constant_velocity_gather():
+    g = np.load(os.path.join(GOLDEN, "golden_ref_constant_velocity.npz"))
     nz, nt, d = int(g["nz"]), int(g["nt"]), int(g["d"])
     v = np.full((nz, int(g["nx"])), float(g["v0"]))
     t = np.arange(nt) * float(g["dt"])
