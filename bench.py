@@ -268,7 +268,8 @@ def serving_leg(device, njobs, rate=None, seed=0, kernel="auto"):
     srv.close()
     if err:
         raise err[0]
-    return {"workload": "served shot stream of mixed modeling / RTM jobs on 256x256 to 1024x2048 grids", "jobs": len(sched), "model_jobs": kinds["model"],
+    return {"workload": "served shot stream of mixed modeling / RTM jobs on 256x256 to 1024x2048 grids",
+            "jobs": len(sched), "model_jobs": kinds["model"],
             "rtm_jobs": kinds["rtm"], "arrival_rate_per_s": round(rate, 3),
             "grids": [f"{g[0]}x{g[1]}" for g in workflow.SERVED_GRIDS], "seconds": list(workflow.SERVED_SECONDS),
             "value": round(st["point_updates"] / wall / 1e9, 3), "unit": "Gpts/s",
@@ -297,7 +298,8 @@ def run_ours(args):
         sv.shots = shards.shard(sv.shots, rank, world)
         ctx = mnad.Context(local, snapshot_codec=sv.codec, kernel=args.kernel)
         data_desc = "synthetic (seeded Gaussian random field + dipping reflectors)"
-        wl = {"workload": "batched RTM of 64 shots, 401x1201 Gaussian random field with dipping reflectors", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
+        wl = {"workload": "batched RTM, 401x1201 Gaussian random field with dipping reflectors",
+              "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
               "snapshots": sv.codec, "propagations_per_shot": 3}
     jobs = workflow.shot_jobs(sv, "rtm")
     m0 = ctx.memory()
@@ -467,13 +469,15 @@ def run_reference(args):
             vals.append(sum(r[1] for r in res) / el / 1e9)
         wall = time.perf_counter() - t0
     value = statistics.median(vals)
-    sample = (f"{workers} worker processes (parfor analogue), each one shot of the 401x1201 random-field survey for {args.ref_steps} "
-              f"time steps (401x1201 + 2x40 CPML), literal FP64 sparse-operator restatement (SciPy)")
+    sample = (f"{workers} worker processes (parfor analogue), each one shot of the 401x1201 random-field survey "
+              f"for {args.ref_steps} time steps (401x1201 + 2x40 CPML), literal FP64 sparse-operator "
+              f"restatement (SciPy)")
     line = {"metric": METRIC, "value": round(value, 5), "unit": "Gpts/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(wall * 1e3 / args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Gaussian random field + dipping reflectors)",
-            "config": {"workload": "batched RTM of 64 shots, 401x1201 Gaussian random field with dipping reflectors", "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
+            "config": {"workload": "batched RTM, 401x1201 Gaussian random field with dipping reflectors",
+                       "grid": "401x1201 (+2x40 CPML) @ 12.5 m",
                        "shots": args.shots, "nt": args.nt, "parallelism": f"{workers} host processes"},
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 5), "unit": "Gpts/s", "cores": workers, "kind": "port",
