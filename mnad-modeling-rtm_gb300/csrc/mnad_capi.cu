@@ -142,7 +142,7 @@ MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const d
         Prop p;
         p.spec = s;
         const TileCfg tc = tile_cfg(c.opt.kernel);
-        p.build(c, tc);
+        p.build(c);
         Batch b(c, tc);
         b.add(&p);
         b.finalize();
@@ -186,7 +186,7 @@ MNAD_API int mnad_fwd_fields(mnad_context* ctx, double dx, double xs, const doub
         Prop p;
         p.spec = s;
         const TileCfg tc = tile_cfg(c.opt.kernel);
-        p.build(c, tc);
+        p.build(c);
         Batch b(c, tc);
         b.add(&p);
         b.finalize();
@@ -273,7 +273,7 @@ MNAD_API int mnad_born_adj(mnad_context* ctx, double dx, double dz, int nt, doub
         Prop p;
         p.spec = s;
         const TileCfg tc = tile_cfg(c.opt.kernel);
-        p.build(c, tc);
+        p.build(c);
         upload(c, p.data.get(), data, (size_t)nt * nr * sizeof(double));
         Batch b(c, tc);
         b.add(&p);
@@ -572,7 +572,7 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
             auto it = P->rcache.find(key);
             if (it == P->rcache.end()) it = P->rcache.emplace(key, make_r(c, sp.v, sp.nz, sp.nx, sp.dt, sp.mode)).first;
             p->r_ext = it->second.as<float>();
-            p->build(c, tc);
+            p->build(c);
             (p->spec.mode == MODE_FWD ? P->phase1 : P->phase3)->add(p.get());
             P->pts += p->point_updates();
             P->bytes += p->algorithmic_bytes();

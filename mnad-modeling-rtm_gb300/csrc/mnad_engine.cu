@@ -267,7 +267,7 @@ DevMem make_r(Context& ctx, const double* v, int nz, int nx, double dt, int mode
     return r;
 }
 
-void Prop::build(Context& ctx, const TileCfg& tc)
+void Prop::build(Context& ctx)
 {
     const PropSpec& s = spec;
     const int nz = s.nz, nx = s.nx, d = s.d;
@@ -277,7 +277,6 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     // kernel that overhang the strip (aligned to 16 bytes at both sides).
     const int dpz = (int)round_up((size_t)d + 6, 4);
     const int zb0 = (nz - d) & ~3;
-    cudaStream_t st = ctx.stream;
 
     fields = DevMem(&ctx, 6 * S * sizeof(float));
     if (!r_ext) r = make_r(ctx, s.v, nz, nx, s.dt, s.mode);
@@ -291,7 +290,6 @@ void Prop::build(Context& ctx, const TileCfg& tc)
     D.s_begin = INT_MIN;
     D.s_end = INT_MAX;
     D.mode = s.mode; D.nt = s.nt; D.nz = nz; D.nx = nx; D.ld = ld; D.d = d; D.dpz = dpz; D.zb0 = zb0;
-    (void)tc;
     D.ntz = (nz + TMA_TZ - 1) / TMA_TZ;      // receiver buckets use the TMA tiling for every kernel
     D.ntx = (nx + TMA_TX - 1) / TMA_TX;
     for (int t = 0; t < 2; ++t)

@@ -146,7 +146,7 @@ struct Prop {
     DevMem fields, r, mx, mz, src_amp, rec_pt, rec_id, rec_r, tile_rec, col_rec, data, datav, dataw, image;
     DevMem energy, d_desc;             // energy history; this propagation's descriptor on the device
     const float* r_ext = nullptr;      // set before build(): r shared with other propagations
-    void build(Context& ctx, const TileCfg& tc);
+    void build(Context& ctx);
     void reset(Context& ctx);          // zero the state of a fresh run (stream-ordered)
     void start(Context& ctx, int s_off);   // reset + seed the source; run from global step s_off (even)
     Checkpoints ckpt;

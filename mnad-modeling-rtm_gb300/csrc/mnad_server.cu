@@ -114,7 +114,7 @@ bool mnad_server::admit(ServerJob* j)
         const mnad_job& J = j->job;
         j->fwd_true = std::make_unique<Prop>();
         j->fwd_true->spec = job_spec(J, MODE_FWD, J.v, nullptr, 0, c.opt.pairing);
-        j->fwd_true->build(c, tc);
+        j->fwd_true->build(c);
         j->points = (double)J.nz * J.nx * J.nt;
         if (J.kind == MNAD_JOB_RTM) {
             int ncols;
@@ -122,10 +122,10 @@ bool mnad_server::admit(ServerJob* j)
             j->wf = new_wavefield(c, J.nz, J.nx, J.d_pml, J.nt, j->T, ncols, J.nt / j->T, c.opt.snapshot_codec);
             j->fwd_bg = std::make_unique<Prop>();
             j->fwd_bg->spec = job_spec(J, MODE_FWD, J.vs, j->wf.get(), j->T, c.opt.pairing);
-            j->fwd_bg->build(c, tc);
+            j->fwd_bg->build(c);
             j->adj = std::make_unique<Prop>();
             j->adj->spec = job_spec(J, MODE_ADJ, J.vs, j->wf.get(), j->T, c.opt.pairing);
-            j->adj->build(c, tc);
+            j->adj->build(c);
             j->points *= 3;
         }
         c.budget = budget;
