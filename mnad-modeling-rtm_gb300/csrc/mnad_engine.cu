@@ -119,7 +119,7 @@ void download(Context& ctx, void* dst, const void* src, size_t bytes)
 // ---------------------------------------------------------------------------
 TileCfg tile_cfg(int kernel)
 {
-    return TileCfg{kernel, TMA_TZ, TMA_TX};
+    return TileCfg{kernel};
 }
 
 void bucket_receivers(int nz, int nx, int ld, const std::vector<int>& zr, const std::vector<int>& xr,

@@ -85,8 +85,7 @@ struct Context {
 // kernel below) or MNAD_KERNEL_TUNE (per launch group, measured on the
 // batch's own propagations at its first run; Batch::tune).
 struct TileCfg {
-    int kind;
-    int tz, tx;   // receiver bucket tile: TMA_TZ x TMA_TX for every kernel
+    int kind;     // MNAD_KERNEL_*
 };
 TileCfg tile_cfg(int kernel);
 // Measured crossover of the two step kernels on GB300 (152 SMs, 2 CTAs per
