@@ -120,8 +120,19 @@ MNAD_API int mnad_context_transfers(const mnad_context* ctx, uint64_t* h2d_bytes
  * the MNAD gradient fields).  *n receives the number of entries; at most max
  * are copied to out. */
 MNAD_API int mnad_context_energy(const mnad_context* ctx, double* out, int max, int* n);
-/* Bit set of device-side status flags seen so far (and clears them). */
+/* Bit set of device-side status flags seen so far (and clears them):
+ * 1 = a recorded value was not finite, 2 = an FP16 snapshot saturated,
+ * 4 = a bounded device wait ran out.  Every propagating entry point reads and
+ * clears these flags itself at its end and fails with MNAD_E_NUMERIC (1, 2)
+ * or MNAD_E_TIMEOUT (4) when one is set; the context stays usable. */
 MNAD_API int mnad_context_status(mnad_context* ctx, unsigned* flags);
+/* Bound of every barrier wait in the persistent step kernel, in polls of the
+ * barrier (0: the default, about 4 M polls -- far longer than any tile copy
+ * takes).  A wait that runs out makes the launch give up its remaining
+ * tiles, and the call then returns MNAD_E_TIMEOUT.  A diagnostic for
+ * watchdog tests: a limit of a few polls makes the waits run out on purpose.
+ * No counterpart in the reference (its MATLAB loop has no device waits). */
+MNAD_API int mnad_context_set_wait_limit(mnad_context* ctx, unsigned polls);
 
 /* ---- drop-in entry points (reference call signatures) ------------------- */
 
@@ -160,9 +171,13 @@ MNAD_API int mnad_fwd_fields(mnad_context* ctx, double dx, double xs, const doub
  * the library holds until the process exits; a shot needing more (roughly a
  * 1000 x 1000 padded grid, or a long record with many receivers) is rejected
  * with MNAD_E_ARG.  The first call on a device sets up the array's device
- * address on that device.  Calls share the array, clear it on entry and are
- * serialised by the library; all pointers are host pointers, as in
- * mnad_fwd_pde_exact.  No context is needed. */
+ * address on that device, so that first call should come before any stream
+ * capture on the device.  Calls share the array, clear it on entry and are
+ * serialised by the library (calls that overlapped on the GPU would race on
+ * it); all pointers are host pointers, as in mnad_fwd_pde_exact.  No context
+ * is needed; the calling thread's current device is the same after the call
+ * as before it.  Fails with MNAD_E_NUMERIC when a recorded value is not
+ * finite. */
 MNAD_API int mnad_fwd_pde_exact_noalloc(int device, double dx, double xs, const double* xr, int nr,
                                         double dz, double zs, const double* zr,
                                         const double* v, int nz, int nx, double dt, int nt,

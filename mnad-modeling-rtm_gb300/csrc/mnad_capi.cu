@@ -95,6 +95,14 @@ MNAD_API int mnad_context_energy(const mnad_context* ctx, double* out, int max, 
     });
 }
 
+MNAD_API int mnad_context_set_wait_limit(mnad_context* ctx, unsigned polls)
+{
+    return guard([&] {
+        need(ctx != nullptr, "context is NULL");
+        ctx->wait_limit = polls;
+    });
+}
+
 MNAD_API int mnad_context_status(mnad_context* ctx, unsigned* flags)
 {
     return guard([&] {
@@ -153,7 +161,7 @@ MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const d
         if (s.record_vw && dataw) download(c, dataw, p.dataw.get(), nd * sizeof(double));
         c.last_energy.assign(p.energy.size() / sizeof(double), 0.0);
         if (!c.last_energy.empty()) download(c, c.last_energy.data(), p.energy.get(), p.energy.size());
-        c.sync();
+        check_device_status(c, "mnad_fwd_pde_exact");
         if (wf) c.wavefields[ss] = std::move(wf);
     });
 }
@@ -215,7 +223,7 @@ MNAD_API int mnad_fwd_fields(mnad_context* ctx, double dx, double xs, const doub
         download(c, datau, p.data.get(), (size_t)nt * nr * sizeof(double));
         c.last_energy.assign(p.energy.size() / sizeof(double), 0.0);
         if (!c.last_energy.empty()) download(c, c.last_energy.data(), p.energy.get(), p.energy.size());
-        c.sync();
+        check_device_status(c, "mnad_fwd_fields");
     });
 }
 
@@ -285,7 +293,7 @@ MNAD_API int mnad_born_adj(mnad_context* ctx, double dx, double dz, int nt, doub
                                                                                         out.as<double>());
         MNAD_CK(cudaGetLastError());
         download(c, im, out.get(), n * sizeof(double));   // Im = T*Im (:138)
-        c.sync();
+        check_device_status(c, "mnad_born_adj");
     });
 }
 
@@ -632,6 +640,7 @@ MNAD_API int mnad_plan_run(mnad_plan* P)
         P->fwd_ms = a;
         P->adj_ms = b;
         P->launches = P->phase1->steps() + (P->ckpt ? seg_launches : P->phase3->steps());
+        check_device_status(c, "mnad_plan_run");
     });
 }
 

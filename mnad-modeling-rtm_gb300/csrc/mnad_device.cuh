@@ -29,12 +29,20 @@ enum Codec { CODEC_F32 = 0, CODEC_BF16 = 1, CODEC_F16 = 2 };
 enum SnapFlags { SNAP_WRITE = 1, SNAP_ILLUM = 2 };
 enum Pairing { PAIR_REFERENCE = 0, PAIR_ALIGNED = 1 };
 
-// Status bits written by kernels (never traps).
+// Status bits written by kernels (never traps).  ST_NONFINITE goes to the
+// propagation's own word (PropDesc::status), ST_TIMEOUT to the launch's
+// (StepArgs::status); the host reads both after a run and turns them into
+// MNAD_E_NUMERIC / MNAD_E_TIMEOUT.
 enum StatusBits : unsigned {
-    ST_NONFINITE = 1u,     // a non-finite value was produced
+    ST_NONFINITE = 1u,     // a recorded receiver value was not finite
     ST_F16_RANGE = 2u,     // an FP16 snapshot value saturated
     ST_TIMEOUT = 4u,       // a bounded wait for a tile copy ran out
 };
+
+// Default bound of a barrier wait (polls), and the bound of the wait with
+// which a CTA that gave up lets its own copies in flight land before it exits.
+constexpr unsigned SPIN_LIMIT_DEFAULT = 1u << 22;
+constexpr unsigned DRAIN_LIMIT = 1u << 24;
 
 // The distinct stencil coefficients of one destination point.  Each is
 // alpha*r + beta*r^2 with r = v^2 dt^2 at the destination (the reference's
@@ -45,7 +53,7 @@ enum StatusBits : unsigned {
 //   Auu: 2 - sum_k c_k                        (the row sums to exactly 2)
 //   Avv: 2 - sum_k c_k + (-15 r/dx^2 + 15 r^2/dx^4)   -> K_VV_R
 //   Aww: 2 - sum_k c_k + (-15 r/dz^2 + 15 r^2/dz^4)   -> K_WW_R
-// (sums of Auu_gen.m:30-86, Avv_gen.m:101-157, Aww_gen.m:164-220).  The
+// (sums of Auu_gen.m:30-86, Avv_gen.m:29-85, Aww_gen.m:31-87).  The
 // sign pattern of the odd couplings is applied in mnad_update().
 enum Coef {
     K_UU_Z, K_UU_X, K_UU_D,                  // Auu_gen.m
@@ -144,6 +152,8 @@ struct StepArgs {
     int ntz;               // tiles along z of every propagation of the group
     int tiles_per_prop;    // ntz * ntx (one geometry per launch group)
     int s;                 // global step index
+    unsigned* status;      // launch-wide status word (ST_TIMEOUT: the launch did not finish its tiles)
+    unsigned spin_limit;   // polls of a bounded barrier wait before it gives up (TMA kernel)
 };
 
 // Neighbourhood of one point for the three fields.  Naming: <f><z><x> with
@@ -161,7 +171,7 @@ struct Hood {
 //     r * sum_k alpha_k D_k + r^2 * sum_k beta_k D_k
 // over the neighbour combinations D_k (two FMAs per term, constants from the
 // kernel parameters).  Signs of the odd couplings follow the J index arrays
-// of the generator files (e.g. Auv_gen.m:119-170: +c at i+1, -c at i-1,
+// of the generator files (e.g. Auv_gen.m:27-78: +c at i+1, -c at i-1,
 // +c at i-2, -c at i+2).
 __device__ __forceinline__ void mnad_update(const Coefs& K, float r, const Hood& h,
                                             float& su, float& sv, float& sw)
@@ -183,19 +193,19 @@ __device__ __forceinline__ void mnad_update(const Coefs& K, float r, const Hood&
     const float dVz = (h.vzm + h.vzp) - v2, dVx = (h.vxm + h.vxp) - v2;
     const float vA = h.vmm + h.vpp, vB = h.vpm + h.vmp;
     const float dVd = (vA + vB) - (v2 + v2);
-    const float vX1 = h.vxp - h.vxm;                          // Auv_gen.m:121,128
-    const float vDx = (h.vmp + h.vpp) - (h.vmm + h.vpm);      // Auv_gen.m:135-156
-    const float vX2 = h.vxm2 - h.vxp2;                        // Auv_gen.m:163,170
-    const float vXZ = vA - vB;                                // Awv_gen.m:106-127
+    const float vX1 = h.vxp - h.vxm;                          // Auv_gen.m:29,36
+    const float vDx = (h.vmp + h.vpp) - (h.vmm + h.vpm);      // Auv_gen.m:43-64
+    const float vX2 = h.vxm2 - h.vxp2;                        // Auv_gen.m:71,78
+    const float vXZ = vA - vB;                                // Awv_gen.m:31-52
     // W combinations
     const float w2 = h.w00 + h.w00;
     const float dWz = (h.wzm + h.wzp) - w2, dWx = (h.wxm + h.wxp) - w2;
     const float wA = h.wmm + h.wpp, wB = h.wpm + h.wmp;
     const float dWd = (wA + wB) - (w2 + w2);
-    const float wZ1 = h.wzp - h.wzm;                          // Auw_gen.m:205,212
-    const float wDz = (h.wpm + h.wpp) - (h.wmm + h.wmp);      // Auw_gen.m:219-240
-    const float wZ2 = h.wzm2 - h.wzp2;                        // Auw_gen.m:247,254
-    const float wXZ = wA - wB;                                // Avw_gen.m:192-213
+    const float wZ1 = h.wzp - h.wzm;                          // Auw_gen.m:29,36
+    const float wDz = (h.wpm + h.wpp) - (h.wmm + h.wmp);      // Auw_gen.m:43-64
+    const float wZ2 = h.wzm2 - h.wzp2;                        // Auw_gen.m:71,78
+    const float wXZ = wA - wB;                                // Avw_gen.m:29-50
     // nU row
     float ra = a[K_UU_Z] * dUz;
     ra = fmaf(a[K_UU_X], dUx, ra);

@@ -211,11 +211,11 @@ void stencil_polys(double dx, double dz, float* al, float* be)
     a[K_UU_Z] = (24.0 / 11) / dz2;   b[K_UU_Z] = -(15 / (11 * dz4) + 1 / (dx2 * dz2));
     a[K_UU_X] = (24.0 / 11) / dx2;   b[K_UU_X] = -(15 / (11 * dx4) + 1 / (dx2 * dz2));
     b[K_UU_D] = 1 / (2 * dx2 * dz2);
-    // Auv_gen.m:128 (i+1), 149 (diagonals at i+1), 163 (i-2)
+    // Auv_gen.m:36 (i+1), 57 (diagonals at i+1), 71 (i-2)
     a[K_UV_X1] = (20.0 / 33) / dx;   b[K_UV_X1] = -(47 / (66 * dx3) + 1 / (6 * dx * dz2));
     b[K_UV_D] = 1 / (12 * dx * dz2);
     a[K_UV_X2] = (1.0 / 132) / dx;   b[K_UV_X2] = -(1.0 / 66) / dx3;
-    // Auw_gen.m:205 (j+1), 226 (diagonals at j+1), 254 (j-2)
+    // Auw_gen.m:29 (j+1), 50 (diagonals at j+1), 78 (j-2)
     a[K_UW_Z1] = (20.0 / 33) / dz;   b[K_UW_Z1] = -(47 / (66 * dz3) + 1 / (6 * dz * dx2));
     b[K_UW_D] = 1 / (12 * dz * dx2);
     a[K_UW_Z2] = (1.0 / 132) / dz;   b[K_UW_Z2] = -(1.0 / 66) / dz3;
@@ -223,22 +223,22 @@ void stencil_polys(double dx, double dz, float* al, float* be)
     a[K_VU_X1] = 15 / (2 * dx3) - 1 / (dx * dz2);
     b[K_VU_X1] = -(15 / (2 * dx5) - 1 / (dx * dz4) + 5 / (2 * dx3 * dz2));
     a[K_VU_D] = 1 / (2 * dx * dz2);  b[K_VU_D] = 5 / (4 * dx3 * dz2) - 1 / (2 * dx * dz4);
-    // Avv_gen.m:101,108,115,136
+    // Avv_gen.m:29,36,43,64
     a[K_VV_Z] = 1 / dz2;             b[K_VV_Z] = -2 / (dx2 * dz2);
     a[K_VV_X] = -1.5 / dx2;          b[K_VV_X] = 5 / (2 * dx4) + 1 / (2 * dx2 * dz2);
     // centre -(12/dx^2 + 2/dz^2) r + (10/dx^4 + 4/(dx^2 dz^2)) r^2 minus the
     // off-diagonal sum: the residual of the difference form
     a[K_VV_R] = -15 / dx2;           b[K_VV_R] = 15 / dx4;
     b[K_VV_D] = -1 / (4 * dx2 * dz2);
-    // Avw_gen.m:192 ((j-1,i-1) and (j+1,i+1))
+    // Avw_gen.m:29,50 ((j-1,i-1) and (j+1,i+1))
     a[K_VW] = -1 / (4 * dz * dx);    b[K_VW] = 1 / (4 * dz3 * dx);
     // Awu_gen.m:29 (j-1), 44 (diagonals at j-1)
     a[K_WU_Z1] = 15 / (2 * dz3) - 1 / (dz * dx2);
     b[K_WU_Z1] = -(15 / (2 * dz5) - 1 / (dz * dx4) + 5 / (2 * dz3 * dx2));
     a[K_WU_D] = 1 / (2 * dz * dx2);  b[K_WU_D] = 5 / (4 * dz3 * dx2) - 1 / (2 * dz * dx4);
-    // Awv_gen.m:106 ((j-1,i-1) and (j+1,i+1))
+    // Awv_gen.m:31,52 ((j-1,i-1) and (j+1,i+1))
     a[K_WV] = -1 / (4 * dz * dx);    b[K_WV] = 1 / (4 * dx3 * dz);
-    // Aww_gen.m:164,171,178,199
+    // Aww_gen.m:31,38,45,66
     a[K_WW_Z] = -1.5 / dz2;          b[K_WW_Z] = 5 / (2 * dz4) + 1 / (2 * dx2 * dz2);
     a[K_WW_X] = 1 / dx2;             b[K_WW_X] = -2 / (dz2 * dx2);
     a[K_WW_R] = -15 / dz2;           b[K_WW_R] = 15 / dz4;
@@ -305,7 +305,7 @@ void Prop::build(Context& ctx)
     D.dx = (float)s.dx; D.dz = (float)s.dz; D.dt = (float)s.dt; D.inv_dt = (float)(1.0 / s.dt);
     D.inv_dt2 = (float)(1.0 / (s.dt * s.dt));
     stencil_polys(s.dx, s.dz, coefs.alpha, coefs.beta);
-    D.status = ctx.d_status;
+    D.status = s.status ? s.status : ctx.d_status;
 
     auto off = [&](int j, int i) { return (int)((size_t)(i + HX) * ld + (j + HZ)); };
     D.src = -1;
@@ -720,6 +720,8 @@ void Batch::launch_group(size_t gi, int s, int slot)
         a.ntz = g->ntz;
         a.tiles_per_prop = g->tiles_per_prop;
         a.s = s;
+        a.status = ctx_.d_status;
+        a.spin_limit = ctx_.wait_limit;
         if (g->kind == MNAD_KERNEL_TMA) {
             const size_t smem = step_tma_smem_bytes();
             const int grid = std::min(g->ntiles, ctx_.num_sms * TMA_CTAS_PER_SM);

@@ -65,7 +65,8 @@ struct Context {
     size_t peak = 0;           // largest in_use since creation
     uint64_t h2d = 0, d2h = 0;   // bytes copied host->device / device->host
     int num_sms = 0;
-    unsigned* d_status = nullptr;
+    unsigned* d_status = nullptr;    // launch-wide status word, and every propagation's unless it has its own
+    unsigned wait_limit = 0;         // polls of a bounded barrier wait in the step kernels (0: default)
     std::map<int, std::unique_ptr<Wavefield>> wavefields;
     // MNAD_KERNEL_TUNE: measured step kernel per (nz, nx, d_pml, propagations per launch)
     std::map<std::tuple<int, int, int, int>, int> kernel_choice;
@@ -122,6 +123,7 @@ struct PropSpec {
     int T = 0;                         // snapshot / imaging interval (0: none)
     int pairing = MNAD_PAIR_REFERENCE;
     int energy_every = 0;              // forward: FP64 energy every that many steps
+    unsigned* status = nullptr;        // device status word of this propagation (null: the context's)
 };
 
 // Saved states of a forward propagation (checkpointed RTM).  Slot g - 1

@@ -119,4 +119,20 @@ PropSpec job_spec(const mnad_job& j, int mode, const double* v, Wavefield* wf, i
     return s;
 }
 
+void raise_status(unsigned bits, const std::string& what)
+{
+    if (bits & ST_TIMEOUT)
+        throw Error(MNAD_E_TIMEOUT, what + ": a bounded device wait for a tile copy ran out; the outputs are "
+                                           "incomplete (the context stays usable)");
+    if (bits & ST_NONFINITE)
+        throw Error(MNAD_E_NUMERIC, what + ": a recorded wavefield value is not finite (unstable time step "
+                                           "v*dt/dx, or non-finite input)");
+    if (bits & ST_F16_RANGE) throw Error(MNAD_E_NUMERIC, what + ": an FP16 snapshot value saturated");
+}
+
+void check_device_status(Context& c, const std::string& what)
+{
+    raise_status(c.take_status(), what);
+}
+
 }  // namespace mnad

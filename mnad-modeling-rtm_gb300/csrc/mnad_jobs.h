@@ -45,5 +45,13 @@ std::unique_ptr<Wavefield> new_wavefield(Context& c, int nz, int nx, int d, int 
 void rtm_snapshot_plan(const mnad_job& j, int& T, int& ncols);
 // Propagation spec of a job: forward (true or background model) or adjoint.
 PropSpec job_spec(const mnad_job& j, int mode, const double* v, Wavefield* wf, int T, int pairing);
+// Device status bits -> error: ST_TIMEOUT throws MNAD_E_TIMEOUT (a step
+// launch gave up on a tile copy, so the outputs are incomplete), ST_NONFINITE
+// or ST_F16_RANGE throw MNAD_E_NUMERIC (a recorded value was not finite or a
+// snapshot saturated).  `what` names the call.
+void raise_status(unsigned bits, const std::string& what);
+// Reads and clears the context's status word (synchronising its stream),
+// then raise_status().
+void check_device_status(Context& c, const std::string& what);
 
 }  // namespace mnad

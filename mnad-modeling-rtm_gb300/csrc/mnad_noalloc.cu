@@ -11,8 +11,10 @@
 // Every GPU that loads the library holds that array until the process exits.
 //
 // The first call on a device looks up the array's device address there
-// (cudaGetSymbolAddress with that device current); host code never passes the
-// array's host-side name to a kernel.  All calls share the array and each call
+// (cudaGetSymbolAddress with that device current), so that first call should
+// come before any stream capture on that device; host code never passes the
+// array's host-side name to a kernel.  Each call makes its device current and
+// gives the calling thread its previous current device back on return.  All calls share the array and each call
 // overwrites what the previous one left: the state is cleared at the start of
 // every call, and calls that overlap on the GPU (from several host threads or
 // streams) would race, so this library serialises its own callers with a lock.
@@ -27,6 +29,7 @@
 #include <vector>
 
 #include "mnad_engine.h"
+#include "mnad_jobs.h"
 #include "mnad_kernels.h"
 
 namespace mnad {
@@ -41,6 +44,23 @@ std::mutex g_noalloc_lock;
 void* g_noalloc_addr[MAX_DEVICES] = {};
 
 size_t align256(size_t n) { return (n + 255) / 256 * 256; }
+
+// Makes `device` current for the call and gives the calling thread its own
+// current device back on every exit path (the caller -- a MATLAB session, a
+// host application with its own CUDA work -- keeps the device it had).
+class DeviceScope {
+public:
+    explicit DeviceScope(int device)
+    {
+        MNAD_CK(cudaGetDevice(&prev_));
+        if (prev_ != device) MNAD_CK(cudaSetDevice(device));
+    }
+    ~DeviceScope() { cudaSetDevice(prev_); }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+private:
+    int prev_ = 0;
+};
 
 // Device address of the scratch array on the current device (set-up on the
 // first call per device).
@@ -89,7 +109,7 @@ void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, doub
                                 "entry point has " + std::to_string(NOALLOC_SCRATCH_BYTES) +
                                 " (use mnad_fwd_pde_exact for larger shots)");
     std::lock_guard<std::mutex> guard(g_noalloc_lock);
-    MNAD_CK(cudaSetDevice(device));
+    DeviceScope on(device);
     unsigned char* base = scratch_on(device);
     cudaStream_t st = cudaStreamPerThread;
 
@@ -186,13 +206,17 @@ void fwd_noalloc(int device, double dx, int xs, const std::vector<int>& xr, doub
     a.ntiles = ntiles;
     a.ntz = ntz;
     a.tiles_per_prop = ntiles;
+    a.status = d_status;
     for (int s = 0; s < nt; ++s) {
         a.s = s;
         step_direct<<<ntiles, dim3(DIRECT_TZ, DIRECT_TX), 0, st>>>(a);
     }
     MNAD_CK(cudaGetLastError());
     if (nr > 0) MNAD_CK(cudaMemcpyAsync(datau, d_data, (size_t)nt * nr * sizeof(double), cudaMemcpyDeviceToHost, st));
+    unsigned bits = 0;
+    MNAD_CK(cudaMemcpyAsync(&bits, d_status, sizeof(bits), cudaMemcpyDeviceToHost, st));
     MNAD_CK(cudaStreamSynchronize(st));
+    raise_status(bits, "mnad_fwd_pde_exact_noalloc");
 }
 
 }  // namespace mnad

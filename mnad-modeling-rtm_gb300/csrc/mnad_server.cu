@@ -46,6 +46,7 @@ struct ServerJob {
     // running state
     int phase = 0;                           // 1: forward(s), 2: adjoint
     int T = 0;
+    DevMem dev_status;                       // device status word of this job's propagations
     std::unique_ptr<Wavefield> wf;
     std::unique_ptr<Prop> fwd_true, fwd_bg, adj;
     double points = 0;                       // grid-point updates of the whole job
@@ -100,6 +101,17 @@ static void free_running_state(ServerJob* j)
     j->fwd_bg.reset();
     j->adj.reset();
     j->wf.reset();
+    j->dev_status.reset();
+}
+
+// Reads and clears the job's status word (the stream is synchronised).
+static unsigned take_job_status(Context& c, ServerJob* j)
+{
+    unsigned s = 0;
+    MNAD_CK(cudaMemcpyAsync(&s, j->dev_status.get(), sizeof(s), cudaMemcpyDeviceToHost, c.stream));
+    MNAD_CK(cudaMemsetAsync(j->dev_status.get(), 0, sizeof(unsigned), c.stream));
+    c.sync();
+    return s;
 }
 
 // Admission: every propagation of the job is built (device state allocated)
@@ -112,8 +124,12 @@ bool mnad_server::admit(ServerJob* j)
     c.budget = budget - reserve;
     try {
         const mnad_job& J = j->job;
+        j->dev_status = DevMem(&c, sizeof(unsigned));
+        MNAD_CK(cudaMemsetAsync(j->dev_status.get(), 0, sizeof(unsigned), c.stream));
+        unsigned* st = j->dev_status.as<unsigned>();
         j->fwd_true = std::make_unique<Prop>();
         j->fwd_true->spec = job_spec(J, MODE_FWD, J.v, nullptr, 0, c.opt.pairing);
+        j->fwd_true->spec.status = st;
         j->fwd_true->build(c);
         j->points = (double)J.nz * J.nx * J.nt;
         if (J.kind == MNAD_JOB_RTM) {
@@ -122,9 +138,11 @@ bool mnad_server::admit(ServerJob* j)
             j->wf = new_wavefield(c, J.nz, J.nx, J.d_pml, J.nt, j->T, ncols, J.nt / j->T, c.opt.snapshot_codec);
             j->fwd_bg = std::make_unique<Prop>();
             j->fwd_bg->spec = job_spec(J, MODE_FWD, J.vs, j->wf.get(), j->T, c.opt.pairing);
+            j->fwd_bg->spec.status = st;
             j->fwd_bg->build(c);
             j->adj = std::make_unique<Prop>();
             j->adj->spec = job_spec(J, MODE_ADJ, J.vs, j->wf.get(), j->T, c.opt.pairing);
+            j->adj->spec.status = st;
             j->adj->build(c);
             j->points *= 3;
         }
@@ -170,12 +188,23 @@ static void download_times(Context& c, double* dst, const void* src, size_t n, i
     for (size_t k = 0; k < n; ++k) dst[k] *= (double)T;
 }
 
-// Called when the propagations of the job's current phase are finished.
+// Called when the propagations of the job's current phase are finished.  A
+// non-finite value recorded by one of the job's propagations fails this job
+// only (its own status word).
 void mnad_server::step_phase(ServerJob* j)
 {
     Context& c = *ctx;
     const mnad_job& J = j->job;
     const size_t nd = (size_t)J.nt * J.nr;
+    const unsigned st = take_job_status(c, j);
+    if (st) {
+        try {
+            raise_status(st, "server job " + std::to_string(j->ticket));
+        } catch (const Error& e) {
+            retire(j, e.code, e.what());
+            return;
+        }
+    }
     if (j->phase == 1 && J.kind == MNAD_JOB_MODEL) {
         if (nd && J.data_out) download(c, J.data_out, j->fwd_true->data.get(), nd * sizeof(double));
         c.sync();
@@ -266,7 +295,9 @@ void mnad_server::loop()
             batch->refresh_descs();
             batch->tick(K, opt.no_graphs == 0);
             for (Prop* p : batch->props()) p->desc.s_off -= K;
-            ctx->sync();
+            // a launch that gave up (a bounded wait ran out) left tiles of every
+            // job of this tick unfinished: those jobs fail, later ones run on
+            raise_status(ctx->take_status() & ST_TIMEOUT, "server tick");
             // retire / advance the jobs whose current phase is over
             std::vector<ServerJob*> still;
             for (ServerJob* j : running) {

@@ -29,8 +29,9 @@
 // (j0 + 4, i0 + 2); j0 is a multiple of TMA_TZ, so the innermost coordinate
 // times 4 bytes is a multiple of 16.  Boxes past the end of the array are
 // zero-filled, which is the reference's omitted out-of-grid neighbour.  Every
-// wait is bounded; a wait that runs out sets ST_TIMEOUT and the CTA leaves
-// after giving its own copies in flight a bounded time to land.
+// wait is bounded (StepArgs::spin_limit polls); a wait that runs out sets
+// ST_TIMEOUT in the launch's status word, and the CTA leaves only after the
+// last copy it issued on each stage has landed (itself a bounded wait).
 #include <cuda.h>
 
 #include <cstddef>
@@ -44,7 +45,6 @@ namespace {
 
 constexpr int BZ = TMA_TZ + 8;     // halo box rows (z)
 constexpr int BX = TMA_TX + 4;     // halo box columns (x)
-constexpr unsigned SPIN_LIMIT = 1u << 22;   // bounded mbarrier wait
 
 struct __align__(128) Stage {
     float halo[3][BX][BZ];         // U, V, W with halo
@@ -114,10 +114,12 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
                  : "memory");
 }
 
-// Bounded wait; gives up early once another thread has aborted.
-__device__ __forceinline__ bool wait_bounded(uint64_t* bar, unsigned parity, const volatile int* abort_flag)
+// Bounded wait of at most `limit` polls; gives up early once another thread
+// has aborted.
+__device__ __forceinline__ bool wait_bounded(uint64_t* bar, unsigned parity, const volatile int* abort_flag,
+                                             unsigned limit)
 {
-    for (unsigned it = 0; it < SPIN_LIMIT; ++it) {
+    for (unsigned it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 1023u) == 1023u && *abort_flag) return false;
     }
@@ -532,11 +534,18 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + OFF_FLAG);
     const int tid = threadIdx.x, lane = tid & 31;
     if (smem_addr(smem_raw) & 127u) {       // TMA destinations need aligned stages
-        if (tid == 0 && A.ntiles > 0) atomicOr(A.props[0].status, ST_TIMEOUT);
+        if (tid == 0 && A.ntiles > 0) atomicOr(A.status, ST_TIMEOUT);
         return;
     }
     const int cur = A.s & 1;
+    const unsigned limit = A.spin_limit ? A.spin_limit : SPIN_LIMIT_DEFAULT;
     int next_claim = -1;                    // producer: tile claimed one refill ahead
+    // producer: operations that complete a phase of each stage's full barrier
+    // (a tile's copies, or the arrive of "no tile"); the last of them is the
+    // only one that can still be in flight
+    unsigned fills[TMA_STAGES];
+#pragma unroll
+    for (int k = 0; k < TMA_STAGES; ++k) fills[k] = 0;
     if (tid == 0) {
         for (int k = 0; k < TMA_STAGES; ++k) {
             mbar_init(&full[k], 1);
@@ -552,9 +561,11 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
     }
     __syncthreads();
     if (tid == 0)
+#pragma unroll
         for (int k = 0; k < TMA_STAGES; ++k) {
             if (stage_tile[k] >= 0) issue_tile(A, stage_tile[k], stages[k], &full[k], cur);
             else mbar_arrive(&full[k]);     // releases the consumers: no tile
+            fills[k] = 1;
         }
     const int tzt = tid % TMA_TZY, txt = tid / TMA_TZY;
     const int c = txt + 2, r0 = tzt * TMA_PZ + 4;
@@ -563,8 +574,10 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
     for (int n = 0;; ++n) {
         const int sidx = n % TMA_STAGES;
         const unsigned parity = (unsigned)(n / TMA_STAGES) & 1u;
-        if (!wait_bounded(&full[sidx], parity, abort_flag)) {
-            if (atomicExch((int*)abort_flag, 1) == 0) atomicOr(A.props[0].status, ST_TIMEOUT);
+        // the warp leaves together if any of its lanes' waits ran out (no
+        // lane may be left behind at a warp-wide synchronisation)
+        if (!__all_sync(0xffffffffu, wait_bounded(&full[sidx], parity, abort_flag, limit))) {
+            if (lane == 0 && atomicExch((int*)abort_flag, 1) == 0) atomicOr(A.status, ST_TIMEOUT);
             break;
         }
         const int t = stage_tile[sidx];      // written before the producer's arrive
@@ -779,13 +792,17 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
         // This warp is done with the stage.
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[sidx]);
+        bool gave_up = false;
         if (tid == 0 && producing) {
             // Refill the stage with the tile claimed earlier once every warp
             // has released it; claim the one after that.
-            if (!wait_bounded(&empty[sidx], parity, abort_flag)) {
-                if (atomicExch((int*)abort_flag, 1) == 0) atomicOr(A.props[0].status, ST_TIMEOUT);
-                break;
+            gave_up = !wait_bounded(&empty[sidx], parity, abort_flag, limit);
+            if (gave_up) {
+                if (atomicExch((int*)abort_flag, 1) == 0) atomicOr(A.status, ST_TIMEOUT);
+                producing = false;
             }
+        }
+        if (tid == 0 && producing) {
             const int t2 = next_claim < A.ntiles ? next_claim : -1;
             stage_tile[sidx] = t2;
             if (t2 >= 0) {
@@ -795,14 +812,25 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                 mbar_arrive(&full[sidx]);   // releases the consumers: no tile
                 producing = false;
             }
+#pragma unroll
+            for (int k = 0; k < TMA_STAGES; ++k) fills[k] += k == sidx;
         }
-        __syncwarp();   // warp 0 reconverges after the producer's work
+        // warp 0 reconverges after the producer's work, and leaves together
+        // with it if its wait ran out
+        if (__shfl_sync(0xffffffffu, (int)gave_up, 0)) break;
     }
     if (tid == 0 && *abort_flag) {
-        // let this CTA's copies still in flight land (bounded) before leaving
-        for (int k = 0; k < TMA_STAGES; ++k)
-            for (unsigned it = 0; it < SPIN_LIMIT; ++it)
-                if (mbar_try_wait(&full[k], 0) || mbar_try_wait(&full[k], 1)) break;
+        // A wait ran out.  Before the CTA exits, the last fill issued on each
+        // stage (phase fills[k] - 1 of its full barrier; every earlier phase
+        // completed before the producer could issue the next) must have
+        // landed: a bulk copy must not write into the shared memory of an
+        // exited CTA.  Bounded too, by DRAIN_LIMIT polls.
+#pragma unroll
+        for (int k = 0; k < TMA_STAGES; ++k) {
+            if (fills[k] == 0) continue;
+            const unsigned par = (fills[k] - 1u) & 1u;
+            for (unsigned it = 0; it < DRAIN_LIMIT && !mbar_try_wait(&full[k], par); ++it) __nanosleep(64);
+        }
     }
 }
 

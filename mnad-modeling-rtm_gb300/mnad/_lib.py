@@ -63,6 +63,7 @@ SIGNATURES = {
     "mnad_context_get_options": ([_vp, C.POINTER(Options)], C.c_int),
     "mnad_context_memory": ([_vp, C.POINTER(C.c_size_t)], C.c_int),
     "mnad_context_status": ([_vp, C.POINTER(C.c_uint)], C.c_int),
+    "mnad_context_set_wait_limit": ([_vp, C.c_uint], C.c_int),
     "mnad_context_energy": ([_vp, _dp, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "mnad_context_transfers": ([_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], C.c_int),
     "mnad_fwd_pde_exact": ([_vp, C.c_double, C.c_double, _dp, C.c_int, C.c_double, C.c_double, _dp,

@@ -124,6 +124,10 @@ class Context:
         check(lib().mnad_context_status(self._h, C.byref(f)))
         return f.value
 
+    def set_wait_limit(self, polls: int = 0):
+        """Bound of the step kernel's barrier waits (0: default); see mnad_context_set_wait_limit."""
+        check(lib().mnad_context_set_wait_limit(self._h, int(polls)))
+
     # -- drop-in shots -----------------------------------------------------
     def fwd(self, dx, xs, xr, dz, zs, zr, v, dt, nt, w, d_pml, ss=1, indx=0, record_vw=False):
         """fwd_PDE_exact_MNAD on the GPU; returns datau (nt, nr) or (datau, datav, dataw)."""

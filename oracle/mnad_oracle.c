@@ -72,14 +72,14 @@ static void coefs(double a, double dx, double dz, double dt, coef_t* c)
     c->uu_xp = c->uu_xm;
     c->uu_c = 2 - (48.0/11)*a2*dt2*(1/dx2 + 1/dz2) + (30.0/11)*a4*dt4*(1/dx4 + 1/dz4 + 11/(15*dx2*dz2));
     c->uu_d = a4*dt4/(2*dx2*dz2);
-    /* Auv_gen.m:121,128,135,149,163,170 */
+    /* Auv_gen.m:29,36,43,57,71,78 */
     c->uv_xm = (-20.0/33)*a2*dt2/dx + a4*dt4*(47/(66*dx3) + 1/(6*dx*dz2));
     c->uv_xp = (20.0/33)*a2*dt2/dx - a4*dt4*(47/(66*dx3) + 1/(6*dx*dz2));
     c->uv_dm = -a4*dt4/(12*dx*dz2);         /* neighbours at i-1 */
     c->uv_dp = a4*dt4/(12*dx*dz2);          /* neighbours at i+1 */
     c->uv_x2m = (1.0/132)*a2*dt2/dx - (1.0/66)*a4*dt4/dx3;
     c->uv_x2p = (-1.0/132)*a2*dt2/dx + (1.0/66)*a4*dt4/dx3;
-    /* Auw_gen.m:205,212,219,226,247,254 */
+    /* Auw_gen.m:29,36,43,50,71,78 */
     c->uw_zp = (20.0/33)*a2*dt2/dz - a4*dt4*(47/(66*dz3) + 1/(6*dz*dx2));
     c->uw_zm = (-20.0/33)*a2*dt2/dz + a4*dt4*(47/(66*dz3) + 1/(6*dz*dx2));
     c->uw_dm = -a4*dt4/(12*dz*dx2);         /* neighbours at j-1 */
@@ -91,12 +91,12 @@ static void coefs(double a, double dx, double dz, double dt, coef_t* c)
     c->vu_xp = a4*dt4*(15/(2*dx5) - 1/(dx*dz4) + 5/(2*dx3*dz2)) - a2*dt2*(15/(2*dx3) - 1/(dx*dz2));
     c->vu_dm = a4*dt4*(5/(4*dx3*dz2) - 1/(2*dx*dz4)) + a2*dt2/(2*dx*dz2);
     c->vu_dp = -a4*dt4*(5/(4*dx3*dz2) - 1/(2*dx*dz4)) - a2*dt2/(2*dx*dz2);
-    /* Avv_gen.m:101,108,115,136 */
+    /* Avv_gen.m:29,36,43,64 */
     c->vv_z = a2*dt2/dz2 - 2*a4*dt4/(dx2*dz2);
     c->vv_x = -(3.0/2)*a2*dt2/dx2 + a4*dt4*(5/(2*dx4) + 1/(2*dx2*dz2));
     c->vv_c = 2 - a2*dt2*(12/dx2 + 2/dz2) + a4*dt4*(10/dx4 + 4/(dx2*dz2));
     c->vv_d = -a4*dt4/(4*dx2*dz2);
-    /* Avw_gen.m:192,199: a on (j-1,i-1),(j+1,i+1); b on (j+1,i-1),(j-1,i+1) */
+    /* Avw_gen.m:29,36: a on (j-1,i-1),(j+1,i+1); b on (j+1,i-1),(j-1,i+1) */
     c->vw_a = a4*dt4/(4*dz3*dx) - a2*dt2/(4*dz*dx);
     c->vw_b = -a4*dt4/(4*dz3*dx) + a2*dt2/(4*dz*dx);
     /* Awu_gen.m:29,36,44,51 */
@@ -104,10 +104,10 @@ static void coefs(double a, double dx, double dz, double dt, coef_t* c)
     c->wu_zp = a4*dt4*(15/(2*dz5) - 1/(dz*dx4) + 5/(2*dz3*dx2)) - a2*dt2*(15/(2*dz3) - 1/(dz*dx2));
     c->wu_dm = a4*dt4*(5/(4*dz3*dx2) - 1/(2*dz*dx4)) + a2*dt2*(1/(2*dz*dx2));    /* j-1 */
     c->wu_dp = -a4*dt4*(5/(4*dz3*dx2) - 1/(2*dz*dx4)) - a2*dt2*(1/(2*dz*dx2));   /* j+1 */
-    /* Awv_gen.m:106,113 */
+    /* Awv_gen.m:31,38 */
     c->wv_a = a4*dt4/(4*dx3*dz) - a2*dt2/(4*dz*dx);
     c->wv_b = -a4*dt4/(4*dx3*dz) + a2*dt2/(4*dz*dx);
-    /* Aww_gen.m:164,171,178,199 */
+    /* Aww_gen.m:31,38,45,66 */
     c->ww_z = -(3.0/2)*a2*dt2/dz2 + a4*dt4*(5/(2*dz4) + 1/(2*dx2*dz2));
     c->ww_x = a2*dt2/dx2 - 2*a4*dt4/(dz2*dx2);
     c->ww_c = 2 - a2*dt2*(12/dz2 + 2/dx2) + a4*dt4*(10/dz4 + 4/(dx2*dz2));

@@ -112,7 +112,7 @@ def a_gen(dx, dz, dt, v):
         E(zlo, xhi, -1, 1, lambda a: a**4*dt**4/(2*dx**2*dz**2)),
         E(zhi, xhi, 1, 1, lambda a: a**4*dt**4/(2*dx**2*dz**2)),
     ])
-    # Auv_gen.m:117-170
+    # Auv_gen.m:25-78
     ops["Auv"] = _assemble(nz, nx, [
         E(fz, xlo, 0, -1, lambda a: (-20/33)*a**2*dt**2/dx + a**4*dt**4*(47/(66*dx**3) + 1/(6*dx*dz**2))),
         E(fz, xhi, 0, 1, lambda a: (20/33)*a**2*dt**2/dx - a**4*dt**4*(47/(66*dx**3) + 1/(6*dx*dz**2))),
@@ -123,7 +123,7 @@ def a_gen(dx, dz, dt, v):
         E(fz, (2, X), 0, -2, lambda a: (1/132)*a**2*dt**2/dx - (1/66)*a**4*dt**4/dx**3),
         E(fz, (0, X - 2), 0, 2, lambda a: (-1/132)*a**2*dt**2/dx + (1/66)*a**4*dt**4/dx**3),
     ])
-    # Auw_gen.m:201-254
+    # Auw_gen.m:25-78
     ops["Auw"] = _assemble(nz, nx, [
         E(zhi, fx, 1, 0, lambda a: (20/33)*a**2*dt**2/dz - a**4*dt**4*(47/(66*dz**3) + 1/(6*dz*dx**2))),
         E(zlo, fx, -1, 0, lambda a: (-20/33)*a**2*dt**2/dz + a**4*dt**4*(47/(66*dz**3) + 1/(6*dz*dx**2))),
@@ -143,7 +143,7 @@ def a_gen(dx, dz, dt, v):
         E(zlo, xhi, -1, 1, lambda a: -a**4*dt**4*(5/(4*dx**3*dz**2) - 1/(2*dx*dz**4)) - a**2*dt**2/(2*dx*dz**2)),
         E(zhi, xhi, 1, 1, lambda a: -a**4*dt**4*(5/(4*dx**3*dz**2) - 1/(2*dx*dz**4)) - a**2*dt**2/(2*dx*dz**2)),
     ])
-    # Avv_gen.m:97-157
+    # Avv_gen.m:25-85
     ops["Avv"] = _assemble(nz, nx, [
         E(zlo, fx, -1, 0, lambda a: a**2*dt**2/dz**2 - 2*a**4*dt**4/(dx**2*dz**2)),
         E(fz, xlo, 0, -1, lambda a: -(3/2)*a**2*dt**2/dx**2 + a**4*dt**4*(5/(2*dx**4) + 1/(2*dx**2*dz**2))),
@@ -155,7 +155,7 @@ def a_gen(dx, dz, dt, v):
         E(zlo, xhi, -1, 1, lambda a: -a**4*dt**4/(4*dx**2*dz**2)),
         E(zhi, xhi, 1, 1, lambda a: -a**4*dt**4/(4*dx**2*dz**2)),
     ])
-    # Avw_gen.m:188-213
+    # Avw_gen.m:25-50
     ops["Avw"] = _assemble(nz, nx, [
         E(zlo, xlo, -1, -1, lambda a: a**4*dt**4/(4*dz**3*dx) - a**2*dt**2/(4*dz*dx)),
         E(zhi, xlo, 1, -1, lambda a: -a**4*dt**4/(4*dz**3*dx) + a**2*dt**2/(4*dz*dx)),
@@ -171,14 +171,14 @@ def a_gen(dx, dz, dt, v):
         E(zlo, xhi, -1, 1, lambda a: a**4*dt**4*(5/(4*dz**3*dx**2) - 1/(2*dz*dx**4)) + a**2*dt**2*(1/(2*dz*dx**2))),
         E(zhi, xhi, 1, 1, lambda a: -a**4*dt**4*(5/(4*dz**3*dx**2) - 1/(2*dz*dx**4)) - a**2*dt**2*(1/(2*dz*dx**2))),
     ])
-    # Awv_gen.m:102-127
+    # Awv_gen.m:27-52
     ops["Awv"] = _assemble(nz, nx, [
         E(zlo, xlo, -1, -1, lambda a: a**4*dt**4/(4*dx**3*dz) - a**2*dt**2/(4*dz*dx)),
         E(zhi, xlo, 1, -1, lambda a: -a**4*dt**4/(4*dx**3*dz) + a**2*dt**2/(4*dz*dx)),
         E(zlo, xhi, -1, 1, lambda a: -a**4*dt**4/(4*dx**3*dz) + a**2*dt**2/(4*dz*dx)),
         E(zhi, xhi, 1, 1, lambda a: a**4*dt**4/(4*dx**3*dz) - a**2*dt**2/(4*dz*dx)),
     ])
-    # Aww_gen.m:160-220
+    # Aww_gen.m:27-87
     ops["Aww"] = _assemble(nz, nx, [
         E(zlo, fx, -1, 0, lambda a: -(3/2)*a**2*dt**2/dz**2 + a**4*dt**4*(5/(2*dz**4) + 1/(2*dx**2*dz**2))),
         E(fz, xlo, 0, -1, lambda a: a**2*dt**2/dx**2 - 2*a**4*dt**4/(dz**2*dx**2)),

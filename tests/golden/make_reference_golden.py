@@ -1,7 +1,7 @@
 """Golden fixtures produced by the reference's own MATLAB sources.
 
-Runs SRC/MNAD/*.m and SRC/migration/Born_adj_MNAD.m of the reference
-checkout (path in MNAD_REFERENCE, default /root/reference) under the MATLAB-
+Runs SRC/MNAD/*.m and SRC/migration/Born_adj_MNAD.m of a reference checkout
+(its path is the first argument, or MNAD_REFERENCE) under the MATLAB-
 subset interpreter oracle/mlite.py -- neither MATLAB nor Octave exists here --
 and stores their outputs:
 
@@ -23,7 +23,8 @@ Born_adj_MNAD.m:105-106 (undefined U_r read as U); the adjoint receives the
 data as a cell {data}, as Born_adj_MNAD.m:50 expects.  The Ricker wavelet of
 the drivers (main_Acoustic_RTM.m:138-140) is an input, computed here.
 
-Usage: python tests/golden/make_reference_golden.py
+Usage: python tests/golden/make_reference_golden.py <reference checkout>
+   or: MNAD_REFERENCE=<reference checkout> python tests/golden/make_reference_golden.py
 """
 import os
 import sys
@@ -37,7 +38,7 @@ sys.path.insert(0, os.path.join(ROOT, "mnad-modeling-rtm_gb300"))
 
 from oracle import mlite  # noqa: E402
 
-REF = os.environ.get("MNAD_REFERENCE", "/root/reference")
+REF = None   # the reference checkout, set by main()
 NAMES = ["Auu", "Auv", "Auw", "Avu", "Avv", "Avw", "Awu", "Awv", "Aww"]
 
 
@@ -139,5 +140,14 @@ def main():
     print("constant velocity |data|", np.linalg.norm(c["data"]))
 
 
+def reference_path():
+    path = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MNAD_REFERENCE")
+    if not path or not os.path.isdir(os.path.join(path, "SRC", "MNAD")):
+        sys.exit("usage: make_reference_golden.py <reference checkout>  (or set MNAD_REFERENCE); "
+                 "the checkout must contain SRC/MNAD and SRC/migration")
+    return path
+
+
 if __name__ == "__main__":
+    REF = reference_path()
     main()

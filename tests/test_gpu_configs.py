@@ -56,8 +56,8 @@ def _gpu_rtm(ctx, sv, sh, codec):
     return data, datas, UU, illum, im
 
 
-def _check(name, ctx, sv, shot, codecs):
-    data, bg, im_ref, T = _oracle_rtm(sv, shot, sv.T)
+def _check(name, ctx, sv, shot, codecs, oracle=None):
+    data, bg, im_ref, T = oracle or _oracle_rtm(sv, shot, sv.T)
     for codec in codecs:
         d, ds, UU, illum, im = _gpu_rtm(ctx, sv, shot, codec)
         errs = dict(gather=rel(d, data), gather_bg=rel(ds, bg["datau"]), snapshots=rel(UU, bg["UU"]),
@@ -80,9 +80,43 @@ def test_layered_single_shot_full_size(ctx, kernel):
         ctx.set_options(kernel="auto")
 
 
-def test_random_field_shot_full_size(ctx):
+@pytest.fixture(scope="module")
+def random_field_shot32():
+    """The random-field survey with the FP64 oracle of shot 32 (about 45 s of CPU)."""
     sv = workflow.random_field_survey(nshots=64)
-    _check("random field 481x1281 shot 32", ctx, sv, sv.shots[32], ("f32", "bf16"))
+    data, bg, im_ref, T = _oracle_rtm(sv, sv.shots[32], sv.T)
+    return sv, dict(scattered=data - bg["datau"], illum=bg["illum"], image=im_ref, T=T,
+                    raw=(data, bg, im_ref, T))
+
+
+def test_random_field_shot_full_size(ctx, random_field_shot32):
+    sv, ref = random_field_shot32
+    _check("random field 481x1281 shot 32", ctx, sv, sv.shots[32], ("f32", "bf16"), oracle=ref["raw"])
+
+
+@pytest.mark.parametrize("codec", ["bf16", "f32"])
+def test_random_field_batched_tma_plan_against_the_oracle(random_field_shot32, codec):
+    """The benchmarked path at its size: shots 30-33 of the random-field survey
+    (481 x 1281 padded, 4 s) as one batched plan on the persistent TMA kernel
+    (8 forwards in one launch per step, then 4 adjoints), scattered data
+    formed on the device, BF16 (the benchmark's codec) and FP32 snapshots.
+    Shot 32's scattered gather, illumination and image against the oracle."""
+    sv, ref = random_field_shot32
+    shots = sv.shots[30:34]
+    jobs = workflow.shot_jobs(sv, "rtm", shots=shots, keep_data=True)
+    with mnad.Context(0, kernel="tma", snapshot_codec=codec) as c:
+        plan = c.plan(jobs)
+        plan.run()
+        plan.download()
+        plan.close()
+    j = jobs[2]
+    errs = dict(scattered=rel(j.data, ref["scattered"]), illum=rel(j.illum, ref["illum"]),
+                image=rel(j.image, ref["image"]))
+    print(f"random field batched TMA plan, shot 32, T={ref['T']}, {codec} snapshots: " +
+          ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+    assert errs["scattered"] <= 10 * TOL_GATHER        # a difference of two gathers
+    assert errs["illum"] <= TOL_IMAGE
+    assert errs["image"] <= (TOL_IMAGE if codec == "f32" else TOL_BF16)
 
 
 def _faulted_plan(sv, **opts):

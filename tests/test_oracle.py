@@ -50,7 +50,7 @@ def test_operator_nnz_and_offsets():
 
 
 def test_operator_antisymmetry():
-    """Auv is odd in x and Auw odd in z (Auv_gen.m:121/128, Auw_gen.m:205/212)."""
+    """Auv is odd in x and Auw odd in z (Auv_gen.m:29/128, Auw_gen.m:29/212)."""
     nz, nx = 15, 15
     v = np.full((nz, nx), 2300.0)
     A = P.a_gen(8.0, 11.0, 1e-3, v)
