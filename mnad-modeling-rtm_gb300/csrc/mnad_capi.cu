@@ -50,7 +50,7 @@ MNAD_API int mnad_context_set_options(mnad_context* ctx, const mnad_options* o)
                  o->snapshot_codec == MNAD_SNAP_F16,
              "snapshot_codec must be MNAD_SNAP_F32, MNAD_SNAP_BF16 or MNAD_SNAP_F16");
         need(o->pairing == MNAD_PAIR_REFERENCE || o->pairing == MNAD_PAIR_ALIGNED, "bad pairing");
-        need(o->kernel >= MNAD_KERNEL_AUTO && o->kernel <= MNAD_KERNEL_TUNE, "bad kernel");
+        need(o->kernel >= MNAD_KERNEL_AUTO && o->kernel <= MNAD_KERNEL_TMA2, "bad kernel");
         need(o->energy_every >= 0, "energy_every must be >= 0");
         need(o->checkpoint_every >= 0, "checkpoint_every must be >= 0");
         need(o->checkpoint_codec == MNAD_SNAP_F32 || o->checkpoint_codec == MNAD_SNAP_F16,
@@ -149,9 +149,10 @@ MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const d
         }
         Prop p;
         p.spec = s;
+        p.spec.depth2 = may_use_depth2(c);
         const TileCfg tc = tile_cfg(c.opt.kernel);
         p.build(c);
-        Batch b(c, tc);
+        Batch b(c, tc, p.spec.depth2);
         b.add(&p);
         b.finalize();
         b.run(use_graph(c, nt));
@@ -280,10 +281,11 @@ MNAD_API int mnad_born_adj(mnad_context* ctx, double dx, double dz, int nt, doub
         s.pairing = c.opt.pairing;
         Prop p;
         p.spec = s;
+        p.spec.depth2 = may_use_depth2(c);
         const TileCfg tc = tile_cfg(c.opt.kernel);
         p.build(c);
         upload(c, p.data.get(), data, (size_t)nt * nr * sizeof(double));
-        Batch b(c, tc);
+        Batch b(c, tc, p.spec.depth2);
         b.add(&p);
         b.finalize();
         b.run(use_graph(c, nt));
@@ -437,6 +439,7 @@ static Prop* add_prop(mnad_plan& P, const mnad_job& j, int mode, const double* v
 {
     auto p = std::make_unique<Prop>();
     p->spec = job_spec(j, mode, v, wf, T, P.ctx->opt.pairing);
+    p->spec.depth2 = !P.ckpt && may_use_depth2(*P.ctx);
     P.props.push_back(std::move(p));
     return P.props.back().get();
 }
@@ -536,12 +539,15 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
         P->jobs.assign(jobs, jobs + njobs);
         for (int k = 0; k < njobs; ++k) check_job(jobs[k], k);
         const TileCfg tc = tile_cfg(c.opt.kernel);
-        P->phase1 = std::make_unique<Batch>(c, tc);
-        P->phase3 = std::make_unique<Batch>(c, tc);
+        P->ckpt = c.opt.checkpoint_every > 0;
+        // whole runs from step 0: the phases may use the two-step kernel
+        // (the checkpointed adjoint runs in step windows, so it may not)
+        const bool d2 = !P->ckpt && may_use_depth2(c);
+        P->phase1 = std::make_unique<Batch>(c, tc, d2);
+        P->phase3 = std::make_unique<Batch>(c, tc, d2);
         P->fwd_true.assign(njobs, nullptr);
         P->fwd_bg.assign(njobs, nullptr);
         P->adj.assign(njobs, nullptr);
-        P->ckpt = c.opt.checkpoint_every > 0;
         P->ck_C.assign(njobs, 0);
         P->ck_m.assign(njobs, 0);
         P->ck_G.assign(njobs, 0);
@@ -639,7 +645,7 @@ MNAD_API int mnad_plan_run(mnad_plan* P)
         P->step_ms = a + b;
         P->fwd_ms = a;
         P->adj_ms = b;
-        P->launches = P->phase1->steps() + (P->ckpt ? seg_launches : P->phase3->steps());
+        P->launches = P->phase1->step_launches() + (P->ckpt ? seg_launches : P->phase3->step_launches());
         check_device_status(c, "mnad_plan_run");
     });
 }

@@ -81,11 +81,15 @@ struct __align__(16) PropDesc {
     int s_off;         // global step at which this propagation started (even)
     int s_begin, s_end;  // global steps [s_begin, s_end) in which it may advance
     int ntz, ntx;      // receiver-bucket (TMA_TZ x TMA_TX) tiles along z / x
-    float* fld[2][3];  // [time level][U,V,W], storage origin (halo included)
+    float* fld[4][3];  // [time level][U,V,W], storage origin (halo included); the
+                       // one-step kernels keep level s & 1, the two-step kernel
+                       // level s & 3 (levels 2, 3 are null without its storage)
     const float* r;    // v^2 dt^2, same storage
     float* mx;         // x-strip memory variables [side 2][var 9][d][ld]
     float* mz;         // z-strip memory variables [side 2][var 9][nx][dpz]; top side slot k
                        // holds row k, bottom side slot k holds row zb0 + k
+    float* mx2;        // second bank of both (two-step kernel only, else null)
+    float* mz2;
     float kx, kz;      // 3 ln(1/R) / (2 D^3), D = d*dx or d*dz (C_cof.m:6,38)
     float dx, dz, dt, inv_dt;
     // source (forward): storage offset of the point and the amount

@@ -54,6 +54,7 @@ Context::Context(int dev, size_t budget_bytes) : device(dev), budget(budget_byte
     uint64_t keep = UINT64_MAX;   // keep freed blocks cached for the next job
     MNAD_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
     MNAD_CK(cudaFuncSetAttribute(step_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_tma_smem_bytes()));
+    MNAD_CK(cudaFuncSetAttribute(step_tma2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_tma2_smem_bytes()));
     MNAD_CK(cudaMalloc(&d_status, sizeof(unsigned)));
     MNAD_CK(cudaMemset(d_status, 0, sizeof(unsigned)));
     opt.snapshot_codec = MNAD_SNAP_F32;
@@ -278,11 +279,16 @@ void Prop::build(Context& ctx)
     const int dpz = (int)round_up((size_t)d + 6, 4);
     const int zb0 = (nz - d) & ~3;
 
-    fields = DevMem(&ctx, 6 * S * sizeof(float));
+    const int levels = s.depth2 ? 4 : 2;
+    fields = DevMem(&ctx, (size_t)levels * 3 * S * sizeof(float));
     if (!r_ext) r = make_r(ctx, s.v, nz, nx, s.dt, s.mode);
     if (d > 0) {
         mx = DevMem(&ctx, (size_t)2 * 9 * d * ld * sizeof(float));
         mz = DevMem(&ctx, (size_t)2 * 9 * nx * dpz * sizeof(float));
+        if (s.depth2) {
+            mx2 = DevMem(&ctx, mx.size());
+            mz2 = DevMem(&ctx, mz.size());
+        }
     }
 
     PropDesc& D = desc;
@@ -292,11 +298,13 @@ void Prop::build(Context& ctx)
     D.mode = s.mode; D.nt = s.nt; D.nz = nz; D.nx = nx; D.ld = ld; D.d = d; D.dpz = dpz; D.zb0 = zb0;
     D.ntz = (nz + TMA_TZ - 1) / TMA_TZ;      // receiver buckets use the TMA tiling for every kernel
     D.ntx = (nx + TMA_TX - 1) / TMA_TX;
-    for (int t = 0; t < 2; ++t)
+    for (int t = 0; t < levels; ++t)
         for (int f = 0; f < 3; ++f) D.fld[t][f] = fields.as<float>() + (size_t)(t * 3 + f) * S;
     D.r = r_ext ? r_ext : r.as<float>();
     D.mx = mx.as<float>();
     D.mz = mz.as<float>();
+    D.mx2 = mx2.as<float>();
+    D.mz2 = mz2.as<float>();
     const double R = 1e-4;   // fwd_PDE_exact_MNAD.m:88
     if (d > 0) {
         D.kx = (float)((3 * std::log(1 / R)) / (2 * std::pow(d * s.dx, 3)));
@@ -386,8 +394,8 @@ void Prop::reset(Context& ctx)
 {
     cudaStream_t st = ctx.stream;
     MNAD_CK(cudaMemsetAsync(fields.get(), 0, fields.size(), st));
-    if (mx.get()) MNAD_CK(cudaMemsetAsync(mx.get(), 0, mx.size(), st));
-    if (mz.get()) MNAD_CK(cudaMemsetAsync(mz.get(), 0, mz.size(), st));
+    for (DevMem* m : {&mx, &mz, &mx2, &mz2})
+        if (m->get()) MNAD_CK(cudaMemsetAsync(m->get(), 0, m->size(), st));
     if (spec.mode == MODE_FWD) {
         if (data.get()) MNAD_CK(cudaMemsetAsync(data.get(), 0, data.size(), st));
         if (desc.illum) MNAD_CK(cudaMemsetAsync(desc.illum, 0, nint() * sizeof(double), st));
@@ -415,7 +423,8 @@ void Prop::setup_checkpoints(Context& ctx, int C, int G, int codec)
     k.C = C;
     k.G = G;
     k.codec = codec;
-    const size_t nf = fields.size() / sizeof(float), nmx = mx.size() / sizeof(float), nmz = mz.size() / sizeof(float);
+    if (spec.depth2) throw Error(MNAD_E_STATE, "checkpointed propagations run the one-step kernels only");
+    const size_t nf = 6 * S, nmx = mx.size() / sizeof(float), nmz = mz.size() / sizeof(float);
     k.slot = nf + nmx + nmz;
     k.blocks.clear();
     for (int b = 0; b < 6; ++b) k.blocks.emplace_back((size_t)b * S, S);                 // U, V, W x 2 levels
@@ -432,10 +441,12 @@ void Prop::setup_checkpoints(Context& ctx, int C, int G, int codec)
     }
 }
 
-// The state arrays of a propagation in slot order: fields, mx, mz.
+// The state arrays of a propagation in slot order: the two time levels of
+// the one-step kernels, mx, mz (checkpointed propagations never run the
+// two-step kernel).
 static void state_parts(Prop& p, float* part[3], size_t count[3])
 {
-    part[0] = p.fields.as<float>(); count[0] = p.fields.size() / sizeof(float);
+    part[0] = p.fields.as<float>(); count[0] = 6 * p.S;
     part[1] = p.mx.as<float>();     count[1] = p.mx.size() / sizeof(float);
     part[2] = p.mz.as<float>();     count[2] = p.mz.size() / sizeof(float);
 }
@@ -569,7 +580,8 @@ void Batch::finalize()
     }
     for (auto& g : groups_) {
         g->kind = pick_kind(*g);
-        const bool tma = g->kind == MNAD_KERNEL_TMA;
+        const bool tma2 = g->kind == MNAD_KERNEL_TMA2;
+        const bool tma = g->kind == MNAD_KERNEL_TMA || tma2;
         g->ntz = tma ? (g->nz + TMA_TZ - 1) / TMA_TZ : (g->nz + DIRECT_TZ - 1) / DIRECT_TZ;
         g->tiles_per_prop = g->ntz * (tma ? (g->nx + TMA_TX - 1) / TMA_TX : (g->nx + DIRECT_TX - 1) / DIRECT_TX);
         std::vector<PropDesc> descs;
@@ -585,23 +597,47 @@ void Batch::finalize()
             all.push_back(D);
             if (!tma) continue;
             const int ncols = D.nx + 2 * HX;
-            for (int t = 0; t < 2; ++t)
-                for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ + 8, TMA_TX + 4));
-            for (int t = 0; t < 2; ++t)
-                for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ, TMA_TX));
-            maps.push_back(field_map(D.r, D.ld, ncols, TMA_TZ, TMA_TX));
+            if (tma2) {
+                for (int t = 0; t < 4; ++t)
+                    for (int f = 0; f < 3; ++f)
+                        maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA2_BOX_Z, TMA2_BOX_X_CUR));
+                for (int t = 0; t < 4; ++t)
+                    for (int f = 0; f < 3; ++f)
+                        maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA2_BOX_Z, TMA2_BOX_X_RING));
+                maps.push_back(field_map(D.r, D.ld, ncols, TMA2_BOX_Z, TMA2_BOX_X_RING));
+            } else {
+                for (int t = 0; t < 2; ++t)
+                    for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ + 8, TMA_TX + 4));
+                for (int t = 0; t < 2; ++t)
+                    for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ, TMA_TX));
+                maps.push_back(field_map(D.r, D.ld, ncols, TMA_TZ, TMA_TX));
+            }
+            // The region whose points a tile computes: the tile itself (one
+            // step per pass), or the tile and a ring of 2 points, as rows
+            // j0-4 .. j0+67 and columns i0-2 .. i0+17 (two steps per pass).
+            const int rz0 = tma2 ? -4 : 0, rz1 = tma2 ? TMA_TZ + 4 : TMA_TZ;
+            const int rx0 = tma2 ? -2 : 0, rx1 = tma2 ? TMA_TX + 2 : TMA_TX;
+            // tiles whose region holds a receiver (the adjoint injects there)
+            std::vector<char> rec_in(tma2 ? (size_t)D.ntz * D.ntx : 0, 0);
+            for (size_t e = 0; tma2 && e < p->spec.zr.size(); ++e) {
+                const int zr = p->spec.zr[e], xr = p->spec.xr[e];
+                for (int tx = std::max(0, (xr - rx1) / TMA_TX); tx < D.ntx && tx * TMA_TX + rx0 <= xr; ++tx)
+                    for (int tz = std::max(0, (zr - rz1) / TMA_TZ); tz < D.ntz && tz * TMA_TZ + rz0 <= zr; ++tz)
+                        if (xr < tx * TMA_TX + rx1 && zr < tz * TMA_TZ + rz1) rec_in[(size_t)tz + (size_t)tx * D.ntz] = 1;
+            }
             for (int tx = 0; tx < D.ntx; ++tx)
                 for (int tz = 0; tz < D.ntz; ++tz) {
                     const int j0 = tz * TMA_TZ, i0 = tx * TMA_TX, d = D.d;
-                    const bool interior = j0 >= d && j0 + TMA_TZ <= D.nz - d && i0 >= d && i0 + TMA_TX <= D.nx - d;
+                    const bool interior = j0 + rz0 >= d && j0 + rz1 <= D.nz - d && i0 + rx0 >= d && i0 + rx1 <= D.nx - d;
                     const int tl = tz + tx * D.ntz;
                     const int rb = p->tile_rec_host[tl], re = p->tile_rec_host[tl + 1];
                     if (j0 >= (1 << 16) || i0 >= (1 << 15)) throw Error(MNAD_E_ARG, "grid too large for the TMA tiling");
-                    // the source, or a z/x neighbour whose CPML term sees it
+                    // the source in the region, or next to it (the CPML term of a neighbour sees it)
                     const int zs = p->spec.zs, xs = p->spec.xs;
-                    const bool src = D.src >= 0 && zs >= j0 - 1 && zs <= j0 + TMA_TZ && xs >= i0 - 1 &&
-                                     xs <= i0 + TMA_TX;
-                    info.push_back(make_int4(rb, re, (interior ? 0 : TILE_STRIP) | (re > rb ? TILE_RECEIVERS : 0) |
+                    const bool src = D.src >= 0 && zs >= j0 + rz0 - 1 && zs <= j0 + rz1 && xs >= i0 + rx0 - 1 &&
+                                     xs <= i0 + rx1;
+                    const bool rec = re > rb || (tma2 && rec_in[tl]);
+                    info.push_back(make_int4(rb, re, (interior ? 0 : TILE_STRIP) | (rec ? TILE_RECEIVERS : 0) |
                                                          (src ? TILE_SOURCE : 0),
                                              j0 | (i0 << 16)));
                 }
@@ -626,13 +662,27 @@ void Batch::finalize()
 
 // The group's step kernel: forced, a tuning trial, a measured choice, or the
 // crossover rule.
+// The two-step kernel needs its storage on every propagation of the group,
+// whole runs from step 0 without step windows, and no per-step host work
+// (FP16 snapshot encodes, energy, checkpoints run between single steps).
+bool Batch::depth2_allowed(const LaunchGroup& g) const
+{
+    if (!depth2_ok_ || has_step_hooks()) return false;
+    for (const Prop* p : g.props)
+        if (!p->spec.depth2) return false;
+    return true;
+}
+
 int Batch::pick_kind(const LaunchGroup& g) const
 {
-    if (tc_.kind == MNAD_KERNEL_DIRECT || tc_.kind == MNAD_KERNEL_TMA) return tc_.kind;
+    const bool d2 = depth2_allowed(g);
+    auto valid = [&](int k) { return k == MNAD_KERNEL_TMA2 && !d2 ? MNAD_KERNEL_TMA : k; };
+    if (tc_.kind == MNAD_KERNEL_DIRECT || tc_.kind == MNAD_KERNEL_TMA || tc_.kind == MNAD_KERNEL_TMA2)
+        return valid(tc_.kind);
     if (tc_.kind == MNAD_KERNEL_TUNE) {
-        if (trial_kind_ >= 0) return trial_kind_;
+        if (trial_kind_ >= 0) return valid(trial_kind_);
         auto it = ctx_.kernel_choice.find(std::make_tuple(g.nz, g.nx, g.d, (int)g.props.size()));
-        if (it != ctx_.kernel_choice.end()) return it->second;
+        if (it != ctx_.kernel_choice.end()) return valid(it->second);
     }
     const double tiles = (double)g.props.size() * ((g.nz + TMA_TZ - 1) / TMA_TZ) * ((g.nx + TMA_TX - 1) / TMA_TX);
     return tiles >= AUTO_TMA_TILES_PER_CTA * ctx_.num_sms * TMA_CTAS_PER_SM ? MNAD_KERNEL_TMA : MNAD_KERNEL_DIRECT;
@@ -648,12 +698,18 @@ void Batch::tune()
         known &= ctx_.kernel_choice.count(std::make_tuple(g->nz, g->nx, g->d, (int)g->props.size())) > 0;
     if (known || K < 2 || ntiles_ == 0) return;     // cached, or too short to measure: the rule stands
     const int ng = (int)groups_.size();
-    const int kinds[2] = {MNAD_KERNEL_DIRECT, MNAD_KERNEL_TMA};
-    std::vector<double> ms[2];
+    // candidates: one thread per point, the persistent kernel at one and (where
+    // the batch allows it) at two steps per pass; the two-step kernel launches
+    // at even steps only, so its K steps are timed in K/2 launches
+    bool any_d2 = false;
+    for (const auto& g : groups_) any_d2 |= depth2_allowed(*g);
+    const int kinds[3] = {MNAD_KERNEL_DIRECT, MNAD_KERNEL_TMA, MNAD_KERNEL_TMA2};
+    const int nk = any_d2 ? 3 : 2;
+    std::vector<double> ms[3];
     std::vector<cudaEvent_t> ev((size_t)2 * K * ng, nullptr);
     for (auto& e : ev) MNAD_CK(cudaEventCreate(&e));
     try {
-        for (int c = 0; c < 2; ++c) {
+        for (int c = 0; c < nk; ++c) {
             trial_kind_ = kinds[c];
             finalize();
             start();
@@ -687,8 +743,10 @@ void Batch::tune()
     for (auto& e : ev) cudaEventDestroy(e);
     for (int gi = 0; gi < ng; ++gi) {
         const LaunchGroup& g = *groups_[gi];
-        ctx_.kernel_choice[std::make_tuple(g.nz, g.nx, g.d, (int)g.props.size())] =
-            ms[0][gi] <= ms[1][gi] ? MNAD_KERNEL_DIRECT : MNAD_KERNEL_TMA;
+        int best = 0;
+        for (int c = 1; c < nk; ++c)
+            if (ms[c][gi] < ms[best][gi]) best = c;
+        ctx_.kernel_choice[std::make_tuple(g.nz, g.nx, g.d, (int)g.props.size())] = kinds[best];
     }
     trial_kind_ = -1;
     finalize();
@@ -704,6 +762,7 @@ void Batch::launch_group(size_t gi, int s, int slot)
     {
         auto& g = groups_[gi];
         if (g->ntiles == 0) return;
+        if (g->kind == MNAD_KERNEL_TMA2 && (s & 1)) return;   // step s ran in the launch at s - 1
         StepArgs a;
         a.coef = g->coefs;
         for (int k = 0; k < NCOEF; ++k) {
@@ -722,11 +781,12 @@ void Batch::launch_group(size_t gi, int s, int slot)
         a.s = s;
         a.status = ctx_.d_status;
         a.spin_limit = ctx_.wait_limit;
-        if (g->kind == MNAD_KERNEL_TMA) {
-            const size_t smem = step_tma_smem_bytes();
-            const int grid = std::min(g->ntiles, ctx_.num_sms * TMA_CTAS_PER_SM);
-            step_tma<<<grid, TMA_THREADS, smem, ctx_.stream>>>(a);
-        } else
+        const int grid = std::min(g->ntiles, ctx_.num_sms * TMA_CTAS_PER_SM);
+        if (g->kind == MNAD_KERNEL_TMA)
+            step_tma<<<grid, TMA_THREADS, step_tma_smem_bytes(), ctx_.stream>>>(a);
+        else if (g->kind == MNAD_KERNEL_TMA2)
+            step_tma2<<<grid, TMA_THREADS, step_tma2_smem_bytes(), ctx_.stream>>>(a);
+        else
             step_direct<<<g->ntiles, dim3(DIRECT_TZ, DIRECT_TX), 0, ctx_.stream>>>(a);
     }
 }
@@ -833,7 +893,7 @@ void Batch::advance(int s0, int s1)
 bool Batch::has_tma() const
 {
     for (const auto& g : groups_)
-        if (g->kind == MNAD_KERNEL_TMA && g->ntiles > 0) return true;
+        if ((g->kind == MNAD_KERNEL_TMA || g->kind == MNAD_KERNEL_TMA2) && g->ntiles > 0) return true;
     return false;
 }
 
@@ -841,6 +901,21 @@ int Batch::launches_per_step() const
 {
     int n = 0;
     for (const auto& g : groups_) n += g->ntiles > 0;
+    return n;
+}
+
+int Batch::step_launches() const
+{
+    int n = 0;
+    for (const auto& g : groups_)
+        if (g->ntiles > 0) n += g->kind == MNAD_KERNEL_TMA2 ? (nsteps_ + 1) / 2 : nsteps_;
+    return n;
+}
+
+int Batch::group_kind_count(int kind) const
+{
+    int n = 0;
+    for (const auto& g : groups_) n += g->ntiles > 0 && g->kind == kind;
     return n;
 }
 

@@ -124,6 +124,8 @@ struct PropSpec {
     int pairing = MNAD_PAIR_REFERENCE;
     int energy_every = 0;              // forward: FP64 energy every that many steps
     unsigned* status = nullptr;        // device status word of this propagation (null: the context's)
+    bool depth2 = false;               // also keep the storage of the two-step kernel (4 field
+                                       // levels, a second bank of CPML memory variables)
 };
 
 // Saved states of a forward propagation (checkpointed RTM).  Slot g - 1
@@ -144,7 +146,7 @@ struct Prop {
     Coefs coefs{};                     // stencil polynomials of (dx, dz)
     size_t S = 0;                      // floats per field in storage
     std::vector<int> tile_rec_host;    // receiver bucket offsets per tile
-    DevMem fields, r, mx, mz, src_amp, rec_pt, rec_id, rec_r, tile_rec, col_rec, data, datav, dataw, image;
+    DevMem fields, r, mx, mz, mx2, mz2, src_amp, rec_pt, rec_id, rec_r, tile_rec, col_rec, data, datav, dataw, image;
     DevMem energy, d_desc;             // energy history; this propagation's descriptor on the device
     const float* r_ext = nullptr;      // set before build(): r shared with other propagations
     void build(Context& ctx);
@@ -172,10 +174,13 @@ struct LaunchGroup {
     int ntz = 0, tiles_per_prop = 0;   // tiling of the group's kernel
 };
 
-// Propagations that advance together: one launch per geometry group and step.
+// Propagations that advance together: one launch per geometry group and step
+// (or, for groups on the two-step kernel, per two steps).  `depth2_ok` lets
+// groups use the two-step kernel: the batch's propagations start at global
+// step 0, advance without step windows and were built with depth2 storage.
 class Batch {
 public:
-    Batch(Context& ctx, const TileCfg& tc) : ctx_(ctx), tc_(tc) {}
+    Batch(Context& ctx, const TileCfg& tc, bool depth2_ok = false) : ctx_(ctx), tc_(tc), depth2_ok_(depth2_ok) {}
     ~Batch();
     void add(Prop* p) { props_.push_back(p); }
     void finalize();
@@ -195,6 +200,8 @@ public:
     bool has_step_hooks() const;       // FP16 snapshot encodes, energy or checkpoints per step
     bool has_tma() const;              // a group runs the TMA kernel
     int launches_per_step() const;     // step-kernel launches of one time step
+    int step_launches() const;         // step-kernel launches of a whole run (run())
+    int group_kind_count(int kind) const;   // launch groups running that kernel
     int group_kind(size_t g) const { return groups_[g]->kind; }
     size_t groups() const { return groups_.size(); }
     int steps() const { return nsteps_; }
@@ -204,12 +211,14 @@ private:
     void launch_step(int s, int slot);
     void launch_group(size_t gi, int s, int slot);
     int pick_kind(const LaunchGroup& g) const;
+    bool depth2_allowed(const LaunchGroup& g) const;
     size_t reserve_counters(int nsteps);   // tile counters for nsteps steps (bytes used)
     void encode_snapshots(int s);      // FP16 codec: encode the snapshots taken at step s
     void energy_after(int s);          // energy diagnostic after step s
     void checkpoint_after(int s);      // checkpointed propagations: save the state after step s
     Context& ctx_;
     TileCfg tc_;
+    bool depth2_ok_ = false;
     int trial_kind_ = -1;              // tune(): kernel forced on every group during a trial
     bool tuned_ = false;
     std::vector<Prop*> props_;

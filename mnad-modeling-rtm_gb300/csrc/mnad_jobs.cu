@@ -135,4 +135,9 @@ void check_device_status(Context& c, const std::string& what)
     raise_status(c.take_status(), what);
 }
 
+bool may_use_depth2(const Context& c)
+{
+    return c.opt.kernel == MNAD_KERNEL_TMA2 || c.opt.kernel == MNAD_KERNEL_TUNE;
+}
+
 }  // namespace mnad

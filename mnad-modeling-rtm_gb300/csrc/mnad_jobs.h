@@ -53,5 +53,8 @@ void raise_status(unsigned bits, const std::string& what);
 // Reads and clears the context's status word (synchronising its stream),
 // then raise_status().
 void check_device_status(Context& c, const std::string& what);
+// Whether propagations built under the context's kernel option should carry
+// the storage of the two-step kernel (it may then be chosen for them).
+bool may_use_depth2(const Context& c);
 
 }  // namespace mnad

@@ -23,6 +23,11 @@ constexpr int TMA_CTAS_PER_SM = 2;
 // Tensor maps of one propagation: halo boxes of U,V,W at both time levels,
 // point boxes of U,V,W at both levels, point box of r.
 constexpr int TMAP_HALO = 0, TMAP_POINT = 6, TMAP_R = 12, TMAPS_PER_PROP = 13;
+// Tensor maps of one propagation for the two-step kernel: U, V, W of the four
+// time levels as 72 x 24 boxes (tile + 4-point halo), the same as 72 x 20 boxes
+// (tile + 2-point ring), r as a 72 x 20 box.
+constexpr int TMAP2_CUR = 0, TMAP2_RING = 12, TMAP2_R = 24, TMAPS_PER_PROP2 = 25;
+constexpr int TMA2_BOX_Z = TMA_TZ + 8, TMA2_BOX_X_CUR = TMA_TX + 8, TMA2_BOX_X_RING = TMA_TX + 4;
 // tile_info.z flags
 constexpr int TILE_STRIP = 1;         // intersects a CPML strip or the grid edge
 constexpr int TILE_RECEIVERS = 2;     // has receivers
@@ -31,6 +36,9 @@ constexpr int TILE_SOURCE = 4;        // the source point or one of its z/x neig
 __global__ void step_direct(const __grid_constant__ StepArgs A);
 __global__ void step_tma(const __grid_constant__ StepArgs A);
 size_t step_tma_smem_bytes();
+// Two time steps (A.s even, and A.s + 1) per launch; see mnad_step_tma2.cu.
+__global__ void step_tma2(const __grid_constant__ StepArgs A);
+size_t step_tma2_smem_bytes();
 __global__ void build_r(const double* __restrict__ v, int nz, int nx, double dt, int adjoint,
                         float* __restrict__ r, int ld);
 __global__ void seed_sources(const PropDesc* __restrict__ props, int n);
