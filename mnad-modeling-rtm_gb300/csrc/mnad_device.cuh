@@ -108,6 +108,8 @@ struct __align__(16) PropDesc {
     double* data;            // [nr][nt] (column-major nt x nr): fwd out / adj in
     double* datav;           // optional fwd outputs
     double* dataw;
+    float* inj;              // adjoint: [nt][nr] injection amounts (float)(rec_r[e] * data(tt, rec_id[e]))
+                             // in bucket entry order, built when the propagation starts
     // snapshots (forward with indx==1) / imaging (adjoint)
     int T;                   // 0: none
     float invT;              // 1/T (exact quotients of tt/T via (tt + 0.5) * invT)

@@ -357,6 +357,10 @@ void Prop::build(Context& ctx)
     }
     D.rec_pt = rec_pt.as<int>(); D.rec_id = rec_id.as<int>(); D.rec_r = rec_r.as<double>();
     D.data = data.as<double>(); D.datav = datav.as<double>(); D.dataw = dataw.as<double>();
+    if (s.mode == MODE_ADJ && nr > 0) {
+        inj = DevMem(&ctx, (size_t)nr * s.nt * sizeof(float));
+        D.inj = inj.as<float>();
+    }
 
     d_desc = DevMem(&ctx, sizeof(PropDesc));
     if (s.mode == MODE_FWD && s.energy_every > 0 && s.nt / s.energy_every > 0)
@@ -401,8 +405,15 @@ void Prop::reset(Context& ctx)
         if (desc.illum) MNAD_CK(cudaMemsetAsync(desc.illum, 0, nint() * sizeof(double), st));
         if (spec.wf && spec.wf->maxbits.get())
             MNAD_CK(cudaMemsetAsync(spec.wf->maxbits.get(), 0, spec.wf->maxbits.size(), st));
-    } else if (image.get()) {
-        MNAD_CK(cudaMemsetAsync(image.get(), 0, image.size(), st));
+    } else {
+        if (image.get()) MNAD_CK(cudaMemsetAsync(image.get(), 0, image.size(), st));
+        if (inj.get()) {
+            const size_t n = inj.size() / sizeof(float);
+            const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)ctx.num_sms * 4);
+            // d_desc holds this propagation's data and receiver tables (uploaded at build)
+            injection_table<<<blocks, 256, 0, st>>>(d_desc.as<PropDesc>());
+            MNAD_CK(cudaGetLastError());
+        }
     }
     if (energy.get()) MNAD_CK(cudaMemsetAsync(energy.get(), 0, energy.size(), st));
 }

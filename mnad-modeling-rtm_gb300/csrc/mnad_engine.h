@@ -148,9 +148,11 @@ struct Prop {
     std::vector<int> tile_rec_host;    // receiver bucket offsets per tile
     DevMem fields, r, mx, mz, mx2, mz2, src_amp, rec_pt, rec_id, rec_r, tile_rec, col_rec, data, datav, dataw, image;
     DevMem energy, d_desc;             // energy history; this propagation's descriptor on the device
+    DevMem inj;                        // adjoint: injection table [nt][nr] (built by reset())
     const float* r_ext = nullptr;      // set before build(): r shared with other propagations
     void build(Context& ctx);
-    void reset(Context& ctx);          // zero the state of a fresh run (stream-ordered)
+    void reset(Context& ctx);          // zero the state of a fresh run; an adjoint also builds
+                                       // its injection table from its (final) data (stream-ordered)
     void start(Context& ctx, int s_off);   // reset + seed the source; run from global step s_off (even)
     Checkpoints ckpt;
     void setup_checkpoints(Context& ctx, int C, int G, int codec);

@@ -80,6 +80,20 @@ __global__ void build_r(const double* __restrict__ v, int nz, int nx, double dt,
     }
 }
 
+// Injection table of an adjoint propagation: row tt holds, in receiver-bucket
+// entry order, the amount r_e * data(tt+1, id_e) that Born_adj_MNAD.m:109-111
+// adds at the receiver after the update of step tt (rounded to float once,
+// exactly as the step kernels would).
+__global__ void injection_table(const PropDesc* __restrict__ desc)
+{
+    const PropDesc& P = *desc;
+    const size_t nr = (size_t)P.nr, n = (size_t)P.nt * nr;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const size_t tt = k / nr, e = k - tt * nr;
+        P.inj[k] = (float)(P.rec_r[e] * P.data[(size_t)P.rec_id[e] * P.nt + tt]);
+    }
+}
+
 // U(zs,xs) of the first step holds r_src*w(1) (the injection of tt=1).
 __global__ void seed_sources(const PropDesc* __restrict__ props, int n)
 {

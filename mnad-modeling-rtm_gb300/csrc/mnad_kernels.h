@@ -42,6 +42,7 @@ size_t step_tma2_smem_bytes();
 __global__ void build_r(const double* __restrict__ v, int nz, int nx, double dt, int adjoint,
                         float* __restrict__ r, int ld);
 __global__ void seed_sources(const PropDesc* __restrict__ props, int n);
+__global__ void injection_table(const PropDesc* __restrict__ desc);
 __global__ void snap_export(const void* __restrict__ snap, int codec, const float* __restrict__ scale,
                             size_t nint, int nsnap, int ncols, double* __restrict__ out);
 __global__ void snap_import(const double* __restrict__ in, int codec, const float* __restrict__ scale,

@@ -204,11 +204,9 @@ __device__ __forceinline__ float adjoint_injection(const PropDesc& P, int tt, in
     float inj = 0.0f;
     if (P.mode != MODE_ADJ || tt >= P.nt) return inj;
     const int beg = __ldg(P.col_rec + c), end = __ldg(P.col_rec + c + 1);
+    const float* row = P.inj + (size_t)tt * P.nr;
     for (int k = beg; k < end; ++k)
-        if (__ldg(P.rec_pt + k) == (int)p) {
-            const int rr = __ldg(P.rec_id + k);
-            inj += (float)(__ldg(P.rec_r + k) * __ldg(P.data + (size_t)rr * P.nt + tt));
-        }
+        if (__ldg(P.rec_pt + k) == (int)p) inj += __ldg(row + k);
     return inj;
 }
 

@@ -309,14 +309,16 @@ __device__ __forceinline__ void record_tile(const PropDesc& P, const float* base
 // Adjoint receiver injection r*data(tt+1) of the TMA_PZ points p.. of local
 // column c of receiver-bucket tile tl: only the entries of that column are
 // scanned, in entry order, so receivers at one point add up in the order of
-// the whole list.
+// the whole list.  The amounts come from the propagation's injection table
+// (row tt), so an entry costs two independent loads.
 __device__ __forceinline__ void injection(const PropDesc& P, int tt, int tl, int c, int p, float* inj)
 {
     const int cb = __ldg(P.col_rec + tl * TMA_TX + c), ce = __ldg(P.col_rec + tl * TMA_TX + c + 1);
+    const float* row = P.inj + (size_t)tt * P.nr;
     for (int e = cb; e < ce; ++e) {
         const int k = __ldg(P.rec_pt + e) - p;
+        const float x = __ldg(row + e);
         if (k < 0 || k >= TMA_PZ) continue;
-        const float x = (float)(__ldg(P.rec_r + e) * __ldg(P.data + (size_t)__ldg(P.rec_id + e) * P.nt + tt));
 #pragma unroll
         for (int q = 0; q < TMA_PZ; ++q)
             if (q == k) inj[q] += x;

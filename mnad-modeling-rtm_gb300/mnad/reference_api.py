@@ -72,8 +72,71 @@ def save_wavefield(ctx: Context, ss: int, nz: int, nx: int, d_pml: int, director
 def load_wavefield(ctx: Context, ss: int, nz: int, nx: int, d_pml: int, nt: int, T: int, directory: str = "."):
     """Read ``Wavefields/UU_<ss>.mat`` back into device storage for shot ``ss``
     (the ``load`` at ``Born_adj_MNAD.m:33``).  Trailing all-zero columns of
-    the reference's preallocated matrix stay part of ``ncols``."""
+    the reference's preallocated matrix stay part of ``ncols``.  The
+    illumination written beside it is stored with it when present."""
     import scipy.io
     UU = scipy.io.loadmat(os.path.join(directory, "Wavefields", f"UU_{ss}.mat"))["UU"]
+    illum = None
+    ipath = os.path.join(directory, "Illuminations", f"illum_{ss}.mat")
+    if os.path.exists(ipath):
+        illum = scipy.io.loadmat(ipath)["illum"].ravel(order="F")
     nsnap = nt // T
-    ctx.wavefield_import(ss, nz, nx, d_pml, nt, T, UU, nsnap=min(nsnap, UU.shape[1]))
+    ctx.wavefield_import(ss, nz, nx, d_pml, nt, T, UU, nsnap=min(nsnap, UU.shape[1]), illum=illum)
+
+
+# Fields of the drivers' ``profile`` struct (SRC/migration/main_Acoustic_RTM.m:64-132,
+# SRC/modeling/main_Acoustic_Data.m), in the order the drivers set them.
+PROFILE_FIELDS = ("fc", "f_max", "dt", "T_max", "dx", "nx", "dz", "nz", "ns")
+
+
+def make_profile(fc, dt, T_max, dx, nx, dz, nz, ns, f_max=None) -> dict:
+    """The drivers' ``profile`` struct as a dict (``f_max = 3 fc`` by default,
+    main_Acoustic_RTM.m:62)."""
+    return {"fc": float(fc), "f_max": float(3.0 * fc if f_max is None else f_max), "dt": float(dt),
+            "T_max": float(T_max), "dx": float(dx), "nx": float(nx), "dz": float(dz), "nz": float(nz),
+            "ns": float(ns)}
+
+
+def _cell_row(items):
+    """A 1 x n MATLAB cell array for scipy.io.savemat."""
+    c = np.empty((1, len(items)), dtype=object)
+    for k, x in enumerate(items):
+        c[0, k] = x
+    return c
+
+
+def save_data(path: str, data, profile: dict):
+    """``save data_MNAD_Acoustic data profile`` (main_Acoustic_RTM.m:183,
+    main_Acoustic_Data.m:179): ``data`` is the 1 x ns cell of the forward's
+    returns, each the 1 x 1 cell ``{datau}``; pass the per-shot ``datau``
+    (nt x nr) arrays or the one-element lists ``fwd_PDE_exact_MNAD`` returns."""
+    import scipy.io
+    shots = [d[0] if isinstance(d, (list, tuple)) else d for d in data]
+    scipy.io.savemat(path, {"data": _cell_row([_cell_row([np.asarray(d, dtype=np.float64)]) for d in shots]),
+                            "profile": {k: profile[k] for k in PROFILE_FIELDS}}, format="5")
+
+
+def save_scattered(path: str, data_sct, profile: dict):
+    """``save data_scattered_MNAD_Acoustic data_sct profile``
+    (main_Acoustic_RTM.m:234): the 1 x ns cell of scattered gathers."""
+    import scipy.io
+    scipy.io.savemat(path, {"data_sct": _cell_row([np.asarray(d, dtype=np.float64) for d in data_sct]),
+                            "profile": {k: profile[k] for k in PROFILE_FIELDS}}, format="5")
+
+
+def load_data(path: str):
+    """(per-shot ``datau`` arrays, profile dict) of a file written by
+    :func:`save_data` or by the reference driver."""
+    import scipy.io
+    m = scipy.io.loadmat(path)
+    cells = m["data"]
+    shots = [np.asarray(cells[0, k][0, 0]) for k in range(cells.shape[1])]
+    prof = m["profile"][0, 0]
+    return shots, {k: float(prof[k][0, 0]) for k in prof.dtype.names}
+
+
+def save_illum_average(path: str, illum):
+    """``save(['./Illuminations/illum_' num2str(0)],'illum')``
+    (main_Acoustic_RTM.m:237-244): the illumination averaged over the shots."""
+    import scipy.io
+    scipy.io.savemat(path, {"illum": np.asarray(illum, dtype=np.float64)}, format="5")
