@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--no-oracle", action="store_true", help="skip the FP64-oracle error of the checked shot")
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, plain and CPU legs")
     ap.add_argument("--ref-steps", type=int, default=12, help="reference arm: time steps per worker sample")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "direct", "tma", "tma2", "tune"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "direct", "tma", "tma_narrow", "tma2", "tune"])
     ap.add_argument("--serve-jobs", type=int, default=512, help="served stream length (0: skip the leg)")
     ap.add_argument("--serve-rate", type=float, default=None, help="arrivals per second (default: from the seed)")
     return ap.parse_args()
@@ -386,7 +386,8 @@ def run_ours(args):
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
             "peak_kind": f"{peak_kind} hbm_gbs",
-            "kernel": {"direct": "mnad::step_direct", "tma2": "mnad::step_tma2"}.get(args.kernel, "mnad::step_tma"),
+            "kernel": {"direct": "mnad::step_direct", "tma2": "mnad::step_tma2",
+                       "tma_narrow": "mnad::step_tma_narrow"}.get(args.kernel, "mnad::step_tma"),
             "algorithmic_bytes_per_launch": abytes / plan.timing()["step_launches"]}
     # the same roofline split by phase (forwards with snapshots; adjoints with imaging)
     ph = plan.phases()

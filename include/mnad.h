@@ -66,18 +66,28 @@ enum { MNAD_PAIR_REFERENCE = 0, MNAD_PAIR_ALIGNED = 1 };
  * size advancing together): the persistent TMA kernel (64 x 16 tiles) once a
  * launch has about 2.25 of its tiles per resident CTA (0.7M point-updates on
  * a 152-SM GB300), the one-thread-per-point kernel (32 x 8 tiles) below.
- * TUNE measures both on each launch group of a plan or job batch at its first
- * run (10 trial steps each, before the run starts from zero state) and keeps
- * the faster; choices are cached in the context per grid, CPML width and
- * propagation count.  The serving loop treats TUNE as AUTO.
+ * TMA_NARROW is the persistent kernel on 64 x 8 tiles (128 threads per CTA,
+ * 4 CTAs per SM); its outputs are bitwise those of TMA.
  * TMA2 is the persistent kernel advancing two time steps per pass (temporal
  * blocking of depth 2: each pass reads the two current time levels and writes
  * the next two, so the field traffic per step falls from 40 to about 26
  * bytes per point).  It serves whole runs of the drop-in calls and of job
  * batches (mnad_run_jobs, plans) without checkpointing, FP16 snapshots or the
- * energy diagnostic; elsewhere TMA2 runs as TMA.  TUNE also measures it where
- * it applies. */
-enum { MNAD_KERNEL_AUTO = 0, MNAD_KERNEL_DIRECT = 1, MNAD_KERNEL_TMA = 2, MNAD_KERNEL_TUNE = 3, MNAD_KERNEL_TMA2 = 4 };
+ * energy diagnostic; elsewhere TMA2 runs as TMA.
+ * TUNE measures the candidates -- one thread per point, TMA (64 x 16 tiles),
+ * TMA_NARROW (64 x 8 tiles), and TMA2 where it applies -- on each launch
+ * group of a plan or job batch at its first run (10 trial steps each, before
+ * the run starts from zero state) and keeps the fastest; choices are cached in
+ * the context per grid, CPML width and propagation count.  The serving loop
+ * treats TUNE as AUTO. */
+enum {
+    MNAD_KERNEL_AUTO = 0,
+    MNAD_KERNEL_DIRECT = 1,
+    MNAD_KERNEL_TMA = 2,
+    MNAD_KERNEL_TUNE = 3,
+    MNAD_KERNEL_TMA2 = 4,
+    MNAD_KERNEL_TMA_NARROW = 5
+};
 
 typedef struct mnad_options {
     int snapshot_codec;   /* MNAD_SNAP_*; default MNAD_SNAP_F32 */

@@ -50,7 +50,7 @@ MNAD_API int mnad_context_set_options(mnad_context* ctx, const mnad_options* o)
                  o->snapshot_codec == MNAD_SNAP_F16,
              "snapshot_codec must be MNAD_SNAP_F32, MNAD_SNAP_BF16 or MNAD_SNAP_F16");
         need(o->pairing == MNAD_PAIR_REFERENCE || o->pairing == MNAD_PAIR_ALIGNED, "bad pairing");
-        need(o->kernel >= MNAD_KERNEL_AUTO && o->kernel <= MNAD_KERNEL_TMA2, "bad kernel");
+        need(o->kernel >= MNAD_KERNEL_AUTO && o->kernel <= MNAD_KERNEL_TMA_NARROW, "bad kernel");
         need(o->energy_every >= 0, "energy_every must be >= 0");
         need(o->checkpoint_every >= 0, "checkpoint_every must be >= 0");
         need(o->checkpoint_codec == MNAD_SNAP_F32 || o->checkpoint_codec == MNAD_SNAP_F16,

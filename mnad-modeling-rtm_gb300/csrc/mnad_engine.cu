@@ -55,6 +55,8 @@ Context::Context(int dev, size_t budget_bytes) : device(dev), budget(budget_byte
     MNAD_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
     MNAD_CK(cudaFuncSetAttribute(step_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_tma_smem_bytes()));
     MNAD_CK(cudaFuncSetAttribute(step_tma2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_tma2_smem_bytes()));
+    MNAD_CK(cudaFuncSetAttribute(step_tma_narrow, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)step_tma_narrow_smem_bytes()));
     MNAD_CK(cudaMalloc(&d_status, sizeof(unsigned)));
     MNAD_CK(cudaMemset(d_status, 0, sizeof(unsigned)));
     opt.snapshot_codec = MNAD_SNAP_F32;
@@ -339,8 +341,9 @@ void Prop::build(Context& ctx)
     tile_rec = DevMem(&ctx, tile_rec_host.size() * sizeof(int));
     upload(ctx, tile_rec.get(), tile_rec_host.data(), tile_rec_host.size() * sizeof(int));
     D.tile_rec = tile_rec.as<int>();
-    col_rec = DevMem(&ctx, rb.col_rec.size() * sizeof(int));
-    upload(ctx, col_rec.get(), rb.col_rec.data(), rb.col_rec.size() * sizeof(int));
+    col_rec_host = rb.col_rec;
+    col_rec = DevMem(&ctx, col_rec_host.size() * sizeof(int));
+    upload(ctx, col_rec.get(), col_rec_host.data(), col_rec_host.size() * sizeof(int));
     D.col_rec = col_rec.as<int>();
     if (nr > 0) {
         rec_pt = DevMem(&ctx, nr * sizeof(int));
@@ -592,9 +595,12 @@ void Batch::finalize()
     for (auto& g : groups_) {
         g->kind = pick_kind(*g);
         const bool tma2 = g->kind == MNAD_KERNEL_TMA2;
-        const bool tma = g->kind == MNAD_KERNEL_TMA || tma2;
+        const bool narrow = g->kind == MNAD_KERNEL_TMA_NARROW;
+        const bool tma = g->kind == MNAD_KERNEL_TMA || tma2 || narrow;
+        const int tx_w = narrow ? TMA_TX_NARROW : TMA_TX;        // tile width of the persistent kernels
+        const int ntx_w = (g->nx + tx_w - 1) / tx_w;
         g->ntz = tma ? (g->nz + TMA_TZ - 1) / TMA_TZ : (g->nz + DIRECT_TZ - 1) / DIRECT_TZ;
-        g->tiles_per_prop = g->ntz * (tma ? (g->nx + TMA_TX - 1) / TMA_TX : (g->nx + DIRECT_TX - 1) / DIRECT_TX);
+        g->tiles_per_prop = g->ntz * (tma ? ntx_w : (g->nx + DIRECT_TX - 1) / DIRECT_TX);
         std::vector<PropDesc> descs;
         std::vector<int> tile_prop;
         std::vector<int4> info;
@@ -618,16 +624,16 @@ void Batch::finalize()
                 maps.push_back(field_map(D.r, D.ld, ncols, TMA2_BOX_Z, TMA2_BOX_X_RING));
             } else {
                 for (int t = 0; t < 2; ++t)
-                    for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ + 8, TMA_TX + 4));
+                    for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ + 8, tx_w + 4));
                 for (int t = 0; t < 2; ++t)
-                    for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ, TMA_TX));
-                maps.push_back(field_map(D.r, D.ld, ncols, TMA_TZ, TMA_TX));
+                    for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ, tx_w));
+                maps.push_back(field_map(D.r, D.ld, ncols, TMA_TZ, tx_w));
             }
             // The region whose points a tile computes: the tile itself (one
             // step per pass), or the tile and a ring of 2 points, as rows
             // j0-4 .. j0+67 and columns i0-2 .. i0+17 (two steps per pass).
             const int rz0 = tma2 ? -4 : 0, rz1 = tma2 ? TMA_TZ + 4 : TMA_TZ;
-            const int rx0 = tma2 ? -2 : 0, rx1 = tma2 ? TMA_TX + 2 : TMA_TX;
+            const int rx0 = tma2 ? -2 : 0, rx1 = tma2 ? TMA_TX + 2 : tx_w;
             // tiles whose region holds a receiver (the adjoint injects there)
             std::vector<char> rec_in(tma2 ? (size_t)D.ntz * D.ntx : 0, 0);
             for (size_t e = 0; tma2 && e < p->spec.zr.size(); ++e) {
@@ -636,12 +642,15 @@ void Batch::finalize()
                     for (int tz = std::max(0, (zr - rz1) / TMA_TZ); tz < D.ntz && tz * TMA_TZ + rz0 <= zr; ++tz)
                         if (xr < tx * TMA_TX + rx1 && zr < tz * TMA_TZ + rz1) rec_in[(size_t)tz + (size_t)tx * D.ntz] = 1;
             }
-            for (int tx = 0; tx < D.ntx; ++tx)
+            for (int tx = 0; tx < ntx_w; ++tx)
                 for (int tz = 0; tz < D.ntz; ++tz) {
-                    const int j0 = tz * TMA_TZ, i0 = tx * TMA_TX, d = D.d;
+                    const int j0 = tz * TMA_TZ, i0 = tx * tx_w, d = D.d;
                     const bool interior = j0 + rz0 >= d && j0 + rz1 <= D.nz - d && i0 + rx0 >= d && i0 + rx1 <= D.nx - d;
-                    const int tl = tz + tx * D.ntz;
-                    const int rb = p->tile_rec_host[tl], re = p->tile_rec_host[tl + 1];
+                    // receiver-bucket tile holding the tile, and the tile's entries
+                    // there (its columns i0 % TMA_TX .. + tx_w of the bucket tile)
+                    const int tl = tz + (i0 / TMA_TX) * D.ntz;
+                    const size_t cb = (size_t)tl * TMA_TX + i0 % TMA_TX;
+                    const int rb = p->col_rec_host[cb], re = p->col_rec_host[cb + tx_w];
                     if (j0 >= (1 << 16) || i0 >= (1 << 15)) throw Error(MNAD_E_ARG, "grid too large for the TMA tiling");
                     // the source in the region, or next to it (the CPML term of a neighbour sees it)
                     const int zs = p->spec.zs, xs = p->spec.xs;
@@ -688,7 +697,8 @@ int Batch::pick_kind(const LaunchGroup& g) const
 {
     const bool d2 = depth2_allowed(g);
     auto valid = [&](int k) { return k == MNAD_KERNEL_TMA2 && !d2 ? MNAD_KERNEL_TMA : k; };
-    if (tc_.kind == MNAD_KERNEL_DIRECT || tc_.kind == MNAD_KERNEL_TMA || tc_.kind == MNAD_KERNEL_TMA2)
+    if (tc_.kind == MNAD_KERNEL_DIRECT || tc_.kind == MNAD_KERNEL_TMA || tc_.kind == MNAD_KERNEL_TMA2 ||
+        tc_.kind == MNAD_KERNEL_TMA_NARROW)
         return valid(tc_.kind);
     if (tc_.kind == MNAD_KERNEL_TUNE) {
         if (trial_kind_ >= 0) return valid(trial_kind_);
@@ -714,9 +724,9 @@ void Batch::tune()
     // at even steps only, so its K steps are timed in K/2 launches
     bool any_d2 = false;
     for (const auto& g : groups_) any_d2 |= depth2_allowed(*g);
-    const int kinds[3] = {MNAD_KERNEL_DIRECT, MNAD_KERNEL_TMA, MNAD_KERNEL_TMA2};
-    const int nk = any_d2 ? 3 : 2;
-    std::vector<double> ms[3];
+    const int kinds[4] = {MNAD_KERNEL_DIRECT, MNAD_KERNEL_TMA, MNAD_KERNEL_TMA_NARROW, MNAD_KERNEL_TMA2};
+    const int nk = any_d2 ? 4 : 3;
+    std::vector<double> ms[4];
     std::vector<cudaEvent_t> ev((size_t)2 * K * ng, nullptr);
     for (auto& e : ev) MNAD_CK(cudaEventCreate(&e));
     try {
@@ -795,6 +805,9 @@ void Batch::launch_group(size_t gi, int s, int slot)
         const int grid = std::min(g->ntiles, ctx_.num_sms * TMA_CTAS_PER_SM);
         if (g->kind == MNAD_KERNEL_TMA)
             step_tma<<<grid, TMA_THREADS, step_tma_smem_bytes(), ctx_.stream>>>(a);
+        else if (g->kind == MNAD_KERNEL_TMA_NARROW)
+            step_tma_narrow<<<std::min(g->ntiles, ctx_.num_sms * TMA_CTAS_PER_SM_NARROW), TMA_TZY * TMA_TX_NARROW,
+                              step_tma_narrow_smem_bytes(), ctx_.stream>>>(a);
         else if (g->kind == MNAD_KERNEL_TMA2)
             step_tma2<<<grid, TMA_THREADS, step_tma2_smem_bytes(), ctx_.stream>>>(a);
         else
@@ -904,7 +917,9 @@ void Batch::advance(int s0, int s1)
 bool Batch::has_tma() const
 {
     for (const auto& g : groups_)
-        if ((g->kind == MNAD_KERNEL_TMA || g->kind == MNAD_KERNEL_TMA2) && g->ntiles > 0) return true;
+        if ((g->kind == MNAD_KERNEL_TMA || g->kind == MNAD_KERNEL_TMA2 || g->kind == MNAD_KERNEL_TMA_NARROW) &&
+            g->ntiles > 0)
+            return true;
     return false;
 }
 

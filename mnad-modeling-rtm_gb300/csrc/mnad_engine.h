@@ -146,6 +146,7 @@ struct Prop {
     Coefs coefs{};                     // stencil polynomials of (dx, dz)
     size_t S = 0;                      // floats per field in storage
     std::vector<int> tile_rec_host;    // receiver bucket offsets per tile
+    std::vector<int> col_rec_host;     // ... and per bucket column (RecBuckets::col_rec)
     DevMem fields, r, mx, mz, mx2, mz2, src_amp, rec_pt, rec_id, rec_r, tile_rec, col_rec, data, datav, dataw, image;
     DevMem energy, d_desc;             // energy history; this propagation's descriptor on the device
     DevMem inj;                        // adjoint: injection table [nt][nr] (built by reset())

@@ -20,6 +20,10 @@ constexpr int TMA_THREADS = TMA_TZY * TMA_TX;
 static_assert(TMA_TZ % DIRECT_TZ == 0 && TMA_TX % DIRECT_TX == 0, "direct tiles must nest in TMA tiles");
 constexpr int TMA_STAGES = 3;         // tiles in flight per CTA
 constexpr int TMA_CTAS_PER_SM = 2;
+// The narrow variant of the persistent kernel: 64 x 8 tiles (each half of a
+// receiver-bucket tile), 128 threads and 2 stages per CTA, 4 CTAs per SM.
+constexpr int TMA_TX_NARROW = 8, TMA_STAGES_NARROW = 2, TMA_CTAS_PER_SM_NARROW = 4;
+static_assert(TMA_TX % TMA_TX_NARROW == 0, "narrow tiles nest in receiver-bucket tiles");
 // Tensor maps of one propagation: halo boxes of U,V,W at both time levels,
 // point boxes of U,V,W at both levels, point box of r.
 constexpr int TMAP_HALO = 0, TMAP_POINT = 6, TMAP_R = 12, TMAPS_PER_PROP = 13;
@@ -36,6 +40,8 @@ constexpr int TILE_SOURCE = 4;        // the source point or one of its z/x neig
 __global__ void step_direct(const __grid_constant__ StepArgs A);
 __global__ void step_tma(const __grid_constant__ StepArgs A);
 size_t step_tma_smem_bytes();
+__global__ void step_tma_narrow(const __grid_constant__ StepArgs A);
+size_t step_tma_narrow_smem_bytes();
 // Two time steps (A.s even, and A.s + 1) per launch; see mnad_step_tma2.cu.
 __global__ void step_tma2(const __grid_constant__ StepArgs A);
 size_t step_tma2_smem_bytes();

@@ -338,7 +338,7 @@ MNAD_API int mnad_server_create(int device, const mnad_server_options* o, mnad_s
         if (S->opt.chunk_steps <= 0) S->opt.chunk_steps = 64;
         S->opt.chunk_steps += S->opt.chunk_steps & 1;   // ticks keep the global step even
         need(S->opt.snapshot_codec >= MNAD_SNAP_F32 && S->opt.snapshot_codec <= MNAD_SNAP_F16, "bad snapshot_codec");
-        need(S->opt.kernel >= MNAD_KERNEL_AUTO && S->opt.kernel <= MNAD_KERNEL_TMA2, "bad kernel");
+        need(S->opt.kernel >= MNAD_KERNEL_AUTO && S->opt.kernel <= MNAD_KERNEL_TMA_NARROW, "bad kernel");
         size_t budget = S->opt.hbm_budget_bytes;
         if (budget == 0) {
             MNAD_CK(cudaSetDevice(device));

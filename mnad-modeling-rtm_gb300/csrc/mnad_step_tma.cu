@@ -44,28 +44,33 @@ namespace {
 
 using namespace tile;
 
-constexpr int BX = TMA_TX + 4;     // halo box columns (x)
-
+// One stage of a tile TMA_TZ x TX points wide (TX = TMA_TX, or a narrower
+// tile that nests in the receiver-bucket tiles).
+template <int TX>
 struct __align__(128) Stage {
+    static constexpr int BX = TX + 4;                 // halo box columns (x)
+    static constexpr int FS = BX * BZ;                // field stride of the halo buffer (floats)
     float halo[3][BX][BZ];         // U, V, W with halo
-    float pts[4][TMA_TX][TMA_TZ];  // pU, pV, pW, r
+    float pts[4][TX][TMA_TZ];      // pU, pV, pW, r
     PropDesc desc;                 // the tile's propagation
-    int4 info;                     // receiver bucket begin/end, flags, j0 | i0 << 16
+    int4 info;                     // receiver entries begin/end, flags, j0 | i0 << 16
+    static constexpr unsigned FIELD_BYTES = sizeof(float) * (3 * BX * BZ + 4 * TX * TMA_TZ);
+    static constexpr unsigned BYTES = FIELD_BYTES + sizeof(PropDesc) + sizeof(int4);
 };
-constexpr int FS = BX * BZ;        // field stride of the halo buffer (floats)
-constexpr unsigned FIELD_BYTES = sizeof(float) * (3 * BX * BZ + 4 * TMA_TX * TMA_TZ);
-constexpr unsigned STAGE_BYTES = FIELD_BYTES + sizeof(PropDesc) + sizeof(int4);
-static_assert(offsetof(Stage, desc) == FIELD_BYTES, "descriptor follows the field boxes");
+static_assert(offsetof(Stage<TMA_TX>, desc) == Stage<TMA_TX>::FIELD_BYTES, "descriptor follows the field boxes");
+static_assert(offsetof(Stage<TMA_TX_NARROW>, desc) == Stage<TMA_TX_NARROW>::FIELD_BYTES,
+              "descriptor follows the field boxes");
 static_assert(sizeof(PropDesc) % 16 == 0, "bulk copies move multiples of 16 bytes");
 
 // Thread 0: fill `stage` with tile t of the launch (one transaction).
-__device__ __forceinline__ void issue_tile(const StepArgs& A, int t, Stage& st, uint64_t* bar, int cur)
+template <int TX>
+__device__ __forceinline__ void issue_tile(const StepArgs& A, int t, Stage<TX>& st, uint64_t* bar, int cur)
 {
     const int pi = t / A.tiles_per_prop;
     const int tl = t - pi * A.tiles_per_prop;
-    const int j0 = (tl % A.ntz) * TMA_TZ, i0 = (tl / A.ntz) * TMA_TX;
+    const int j0 = (tl % A.ntz) * TMA_TZ, i0 = (tl / A.ntz) * TX;
     const CUtensorMap* maps = static_cast<const CUtensorMap*>(A.tmaps) + (size_t)pi * TMAPS_PER_PROP;
-    mbar_expect_tx(bar, STAGE_BYTES);
+    mbar_expect_tx(bar, Stage<TX>::BYTES);
     bulk_load(&st.desc, A.props + pi, sizeof(PropDesc), bar);
     bulk_load(&st.info, A.tile_info + t, sizeof(int4), bar);
 #pragma unroll
@@ -76,24 +81,33 @@ __device__ __forceinline__ void issue_tile(const StepArgs& A, int t, Stage& st, 
     tma_load_2d(&st.pts[3][0][0], maps + TMAP_R, bar, j0 + HZ, i0 + HX);
 }
 
+// Shared-memory layout: NST stages, their full and empty barriers, the tile
+// held by each stage, the abort flag.
+template <int TX, int NST>
+struct Layout {
+    static constexpr size_t FULL = NST * sizeof(Stage<TX>);
+    static constexpr size_t EMPTY = FULL + NST * sizeof(uint64_t);
+    static constexpr size_t TILE = EMPTY + NST * sizeof(uint64_t);
+    static constexpr size_t FLAG = TILE + NST * sizeof(int);
+    static constexpr size_t BYTES = FLAG + 16;
+};
+
 }  // namespace
 
-// Shared-memory layout: TMA_STAGES stages, their full and empty barriers,
-// the tile held by each stage, the abort flag.
-constexpr size_t OFF_FULL = TMA_STAGES * sizeof(Stage);
-constexpr size_t OFF_EMPTY = OFF_FULL + TMA_STAGES * sizeof(uint64_t);
-constexpr size_t OFF_TILE = OFF_EMPTY + TMA_STAGES * sizeof(uint64_t);
-constexpr size_t OFF_FLAG = OFF_TILE + TMA_STAGES * sizeof(int);
-constexpr int NWARPS = TMA_THREADS / 32;
-
-__global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const __grid_constant__ StepArgs A)
+// The kernel body for tiles TMA_TZ x TX with NST stages (TMA_TZY x TX threads).
+template <int TX, int NST>
+__device__ __forceinline__ void step_tma_body(const StepArgs& A)
 {
+    using St = Stage<TX>;
+    using L = Layout<TX, NST>;
+    constexpr int FS = St::FS;
+    constexpr int NWARPS = TMA_TZY * TX / 32;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    Stage* stages = reinterpret_cast<Stage*>(smem_raw);
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + OFF_FULL);
-    uint64_t* empty = reinterpret_cast<uint64_t*>(smem_raw + OFF_EMPTY);
-    volatile int* stage_tile = reinterpret_cast<volatile int*>(smem_raw + OFF_TILE);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + OFF_FLAG);
+    St* stages = reinterpret_cast<St*>(smem_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + L::FULL);
+    uint64_t* empty = reinterpret_cast<uint64_t*>(smem_raw + L::EMPTY);
+    volatile int* stage_tile = reinterpret_cast<volatile int*>(smem_raw + L::TILE);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + L::FLAG);
     const int tid = threadIdx.x, lane = tid & 31;
     if (smem_addr(smem_raw) & 127u) {       // TMA destinations need aligned stages
         if (tid == 0 && A.ntiles > 0) atomicOr(A.status, ST_TIMEOUT);
@@ -105,17 +119,17 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
     // producer: operations that complete a phase of each stage's full barrier
     // (a tile's copies, or the arrive of "no tile"); the last of them is the
     // only one that can still be in flight
-    unsigned fills[TMA_STAGES];
+    unsigned fills[NST];
 #pragma unroll
-    for (int k = 0; k < TMA_STAGES; ++k) fills[k] = 0;
+    for (int k = 0; k < NST; ++k) fills[k] = 0;
     if (tid == 0) {
-        for (int k = 0; k < TMA_STAGES; ++k) {
+        for (int k = 0; k < NST; ++k) {
             mbar_init(&full[k], 1);
             mbar_init(&empty[k], NWARPS);
         }
         fence_mbar_init();
         *abort_flag = 0;
-        for (int k = 0; k < TMA_STAGES; ++k) {
+        for (int k = 0; k < NST; ++k) {
             const int t = atomicAdd(A.tile_counter, 1);
             stage_tile[k] = t < A.ntiles ? t : -1;
         }
@@ -124,8 +138,8 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
     __syncthreads();
     if (tid == 0)
 #pragma unroll
-        for (int k = 0; k < TMA_STAGES; ++k) {
-            if (stage_tile[k] >= 0) issue_tile(A, stage_tile[k], stages[k], &full[k], cur);
+        for (int k = 0; k < NST; ++k) {
+            if (stage_tile[k] >= 0) issue_tile<TX>(A, stage_tile[k], stages[k], &full[k], cur);
             else mbar_arrive(&full[k]);     // releases the consumers: no tile
             fills[k] = 1;
         }
@@ -134,8 +148,8 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
     bool producing = true;
 
     for (int n = 0;; ++n) {
-        const int sidx = n % TMA_STAGES;
-        const unsigned parity = (unsigned)(n / TMA_STAGES) & 1u;
+        const int sidx = n % NST;
+        const unsigned parity = (unsigned)(n / NST) & 1u;
         // the warp leaves together if any of its lanes' waits ran out (no
         // lane may be left behind at a warp-wide synchronisation)
         if (!__all_sync(0xffffffffu, wait_bounded(&full[sidx], parity, abort_flag, limit))) {
@@ -144,13 +158,14 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
         }
         const int t = stage_tile[sidx];      // written before the producer's arrive
         if (t < 0) break;
-        const Stage& st = stages[sidx];
+        const St& st = stages[sidx];
         const PropDesc& P = st.desc;
         const int4 info = st.info;
         // Per-tile scalars in registers.
         const int tt = step_tt(P, A.s);
         const int j0 = info.w & 0xffff, i0 = info.w >> 16;
-        const int tl = j0 / TMA_TZ + (i0 / TMA_TX) * P.ntz;
+        const int tl = j0 / TMA_TZ + (i0 / TMA_TX) * P.ntz;     // receiver-bucket tile
+        const int cb0 = i0 % TMA_TX;                            // its column holding the tile's first
         const int nz = P.nz, nx = P.nx, d = P.d, ld = P.ld, nt = P.nt, mode = P.mode;
         if (tt != 0 && (info.z & TILE_RECEIVERS) && mode == MODE_FWD)
             record_tile<FS>(P, &st.halo[0][0][0], 2, tt, info.x, info.y, j0, i0);
@@ -264,17 +279,17 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                 mnad_update_pairs(A.coef2, win, rr, s2u, s2v, s2w);
             }
             if (!lean) {
-                float cu[Q], cv[Q], cw[Q];
+                float2 cu[2], cv[2], cw[2];
 #pragma unroll
-                for (int k = 0; k < Q; ++k) cu[k] = cv[k] = cw[k] = 0.0f;
+                for (int m = 0; m < 2; ++m) cu[m] = cv[m] = cw[m] = pr(0.0f, 0.0f);
                 cpml_vec<FS>(P, &st.halo[0][0][0], c, r0, tt, j, i, p, has_src, rr, bank, bank, true, cu, cv, cw);
                 // sF -= r * (F1_x + F1_z), per point fmaf(-r, c, s)
 #pragma unroll
                 for (int m = 0; m < 2; ++m) {
                     const float2 nr = pr(-rr[2 * m], -rr[2 * m + 1]);
-                    s2u[m] = pfma(nr, pr(cu[2 * m], cu[2 * m + 1]), s2u[m]);
-                    s2v[m] = pfma(nr, pr(cv[2 * m], cv[2 * m + 1]), s2v[m]);
-                    s2w[m] = pfma(nr, pr(cw[2 * m], cw[2 * m + 1]), s2w[m]);
+                    s2u[m] = pfma(nr, cu[m], s2u[m]);
+                    s2v[m] = pfma(nr, cv[m], s2v[m]);
+                    s2w[m] = pfma(nr, cw[m], s2w[m]);
                 }
             }
             const float4 pu4 = *reinterpret_cast<const float4*>(&st.pts[0][txt][tzt * Q]);
@@ -328,7 +343,7 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
                     float inj[Q];
 #pragma unroll
                     for (int k = 0; k < Q; ++k) inj[k] = 0.0f;
-                    injection(P, tt, tl, txt, p, inj);
+                    injection(P, tt, tl, cb0 + txt, p, inj);
 #pragma unroll
                     for (int k = 0; k < Q; ++k) ou[k] -= inj[k];
                 }
@@ -370,23 +385,37 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const _
             const int t2 = next_claim < A.ntiles ? next_claim : -1;
             stage_tile[sidx] = t2;
             if (t2 >= 0) {
-                issue_tile(A, t2, stages[sidx], &full[sidx], cur);
+                issue_tile<TX>(A, t2, stages[sidx], &full[sidx], cur);
                 next_claim = atomicAdd(A.tile_counter, 1);
             } else {
                 mbar_arrive(&full[sidx]);   // releases the consumers: no tile
                 producing = false;
             }
 #pragma unroll
-            for (int k = 0; k < TMA_STAGES; ++k) fills[k] += k == sidx;
+            for (int k = 0; k < NST; ++k) fills[k] += k == sidx;
         }
         // warp 0 reconverges after the producer's work, and leaves together
         // with it if its wait ran out
         if (__shfl_sync(0xffffffffu, (int)gave_up, 0)) break;
     }
     // a wait ran out: the copies this CTA issued must land before it exits
-    if (tid == 0 && *abort_flag) drain_fills<TMA_STAGES>(full, fills);
+    if (tid == 0 && *abort_flag) drain_fills<NST>(full, fills);
 }
 
-size_t step_tma_smem_bytes() { return OFF_FLAG + 16; }
+// 64 x 16 tiles, 3 stages, 256 threads, 2 CTAs per SM (128 registers).
+__global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma(const __grid_constant__ StepArgs A)
+{
+    step_tma_body<TMA_TX, TMA_STAGES>(A);
+}
+size_t step_tma_smem_bytes() { return Layout<TMA_TX, TMA_STAGES>::BYTES; }
+
+// 64 x 8 tiles (half a receiver-bucket tile), 2 stages, 128 threads, 4 CTAs
+// per SM (128 registers; 4 CTAs of 2 stages fit the SM's shared memory).
+__global__ void __launch_bounds__(TMA_TZY * TMA_TX_NARROW, TMA_CTAS_PER_SM_NARROW)
+    step_tma_narrow(const __grid_constant__ StepArgs A)
+{
+    step_tma_body<TMA_TX_NARROW, TMA_STAGES_NARROW>(A);
+}
+size_t step_tma_narrow_smem_bytes() { return Layout<TMA_TX_NARROW, TMA_STAGES_NARROW>::BYTES; }
 
 }  // namespace mnad

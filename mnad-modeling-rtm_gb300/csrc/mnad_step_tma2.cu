@@ -119,17 +119,17 @@ __device__ __forceinline__ void quad_step(const StepArgs& A, const PropDesc& P, 
         mnad_update_pairs(A.coef2, win, rr, su, sv, sw);
     }
     if (!lean) {
-        float cu[Q], cv[Q], cw[Q];
+        float2 cu[2], cv[2], cw[2];
 #pragma unroll
-        for (int k = 0; k < Q; ++k) cu[k] = cv[k] = cw[k] = 0.0f;
+        for (int m = 0; m < 2; ++m) cu[m] = cv[m] = cw[m] = pr(0.0f, 0.0f);
         cpml_vec<WFS>(P, wbase, wc, r0, tt, j, i, p, src_tile, rr, rd, wr, owned, cu, cv, cw);
         // sF -= r * (F1_x + F1_z), per point fmaf(-r, c, s)
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
             const float2 nr = pr(-rr[2 * m], -rr[2 * m + 1]);
-            su[m] = pfma(nr, pr(cu[2 * m], cu[2 * m + 1]), su[m]);
-            sv[m] = pfma(nr, pr(cv[2 * m], cv[2 * m + 1]), sv[m]);
-            sw[m] = pfma(nr, pr(cw[2 * m], cw[2 * m + 1]), sw[m]);
+            su[m] = pfma(nr, cu[m], su[m]);
+            sv[m] = pfma(nr, cv[m], sv[m]);
+            sw[m] = pfma(nr, cw[m], sw[m]);
         }
     }
     const float4 pu4 = *reinterpret_cast<const float4*>(pbase + pc * BZ + r0);

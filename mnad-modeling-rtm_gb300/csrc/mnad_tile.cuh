@@ -293,7 +293,7 @@ template <int FS>
 __device__ __forceinline__ void record_tile(const PropDesc& P, const float* base, int col0, int tt, int rbeg, int rend,
                                             int j0, int i0)
 {
-    for (int e = rbeg + (int)threadIdx.x; e < rend; e += TMA_THREADS) {
+    for (int e = rbeg + (int)threadIdx.x; e < rend; e += (int)blockDim.x) {
         const int pt = __ldg(P.rec_pt + e);
         const int ic = pt / P.ld, jr = pt - ic * P.ld;              // storage column / row
         const int cx = ic - HX - i0 + col0, rz = jr - HZ - j0 + 4;  // position in the buffer
@@ -326,18 +326,40 @@ __device__ __forceinline__ void injection(const PropDesc& P, int tt, int tl, int
 }
 
 // ---- CPML ---------------------------------------------------------------
-// C_cof.m:6-16 at one point: (c1, c2, c3) of a side from the distance term X
-// (X = 0 outside the strip gives exactly 1, 0, 0).  Approximate reciprocal and
-// square root are used for these damping coefficients only.
-__device__ __forceinline__ void cpml_c(float K, float vel, float X, float dt, float& c1, float& c2, float& c3)
+// C_cof.m:6-16 at a z-pair of points: (c1, c2, c3) of a side from the
+// velocities and the distance terms X (X = 0 outside the strip gives exactly
+// 1, 0, 0), in packed FP32x2.  An approximate reciprocal is used for these
+// damping coefficients only.
+struct CpmlC {
+    float2 c1, c2, c3;
+};
+__device__ __forceinline__ CpmlC cpml_c2(float K, float2 vel, float2 X, float dt)
 {
-    const float s0 = K * vel;
-    const float sig = s0 * (X * X);
-    const float a = sig * (0.5f * dt);
-    const float inv = __fdividef(1.0f, 1.0f + a);
-    c1 = (1.0f - a) * inv;
-    c2 = (2.0f * s0 * X) * dt * inv;
-    c3 = (sig * dt) * inv;
+    const float2 s0 = pmul(pr(K, K), vel);
+    const float2 sig = pmul(s0, pmul(X, X));
+    const float2 a = pmul(sig, pr(0.5f * dt, 0.5f * dt));
+    const float2 den = padd(pr(1.0f, 1.0f), a);
+    const float2 inv = pr(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
+    CpmlC c;
+    c.c1 = pmul(psub(pr(1.0f, 1.0f), a), inv);
+    c.c2 = pmul(pmul(pmul(pmul(pr(2.0f, 2.0f), s0), X), pr(dt, dt)), inv);
+    c.c3 = pmul(pmul(sig, pr(dt, dt)), inv);
+    return c;
+}
+
+// One side of Ux123_gen.m / Uz123_gen.m for one field at a z-pair of points
+// (cpml_mem of the per-point kernels, in packed FP32x2): gr = (behind -
+// ahead) on the low side, (ahead - behind) on the high side; lap = behind -
+// 2 F + ahead.  Updates m1..m3 in place, returns the new m1.
+__device__ __forceinline__ float2 cpml_mem2(const CpmlC& c, float2 ih, float2 ih2, float2 gr, float2 lap, float2& m1,
+                                            float2& m2, float2& m3)
+{
+    const float2 g2 = pmul(pmul(c.c2, ih), gr);
+    const float2 hg = pmul(pr(0.5f, 0.5f), g2);
+    m3 = pfma(c.c1, m3, hg);
+    m2 = padd(pfma(c.c1, m2, g2), pmul(c.c3, pfma(lap, ih2, pr(-m3.x, -m3.y))));
+    m1 = padd(pfma(c.c1, m1, hg), pmul(c.c3, pfma(pmul(pr(2.0f, 2.0f), lap), ih2, pr(-m2.x, -m2.y))));
+    return m1;
 }
 
 // Memory-variable storage of one bank: x strips [side 2][var 9][d][ld],
@@ -377,39 +399,64 @@ __device__ __forceinline__ void prefetch_strip_state(const PropDesc& P, MemBank 
 // rows r0.., of a staged buffer of field stride FS.  Memory variables are read
 // from bank `rd` and, when `store`, written to bank `wr` (the same bank for a
 // kernel that advances one step per pass).  Adds F1_x + F1_z of U, V, W into
-// cu, cv, cw.  U is taken before this step's source injection
-// (fwd_PDE_exact_MNAD.m:95-111): the staged U already holds it.
+// cu, cv, cw (as the z-pairs of points 0,1 and 2,3; packed FP32x2 throughout).
+// U is taken before this step's source injection (fwd_PDE_exact_MNAD.m:95-111):
+// the staged U already holds it.
 template <int FS>
 __device__ __forceinline__ void cpml_vec(const PropDesc& P, const float* fbase, int c, int r0, int tt, int j, int i,
                                          int p, bool has_src, const float* r, MemBank rd, MemBank wr, bool store,
-                                         float* cu, float* cv, float* cw)
+                                         float2* cu, float2* cv, float2* cw)
 {
     constexpr int Q = TMA_PZ;
     const int d = P.d, nz = P.nz, nx = P.nx, ld = P.ld;
-    float vel[Q];
+    if (d <= 0) return;                 // no CPML strips (and no memory-variable storage)
+    float2 vel[2];
 #pragma unroll
-    for (int k = 0; k < Q; ++k) vel[k] = r[k] * rsqrtf(r[k]) * P.inv_dt;
+    for (int m = 0; m < 2; ++m)
+        vel[m] = pmul(pmul(pr(r[2 * m], r[2 * m + 1]), pr(rsqrtf(r[2 * m]), rsqrtf(r[2 * m + 1]))),
+                      pr(P.inv_dt, P.inv_dt));
     const float srcamp = (has_src && P.mode == MODE_FWD && P.src >= 0) ? P.src_amp[tt - 1] : 0.0f;
     const int src = P.src;
-    if (d <= 0) return;                 // no CPML strips (and no memory-variable storage)
+    // One field's term of one direction: F0 at the points, Fa / Fd ahead /
+    // behind along the direction (staged, pre-injection values); mv holds
+    // m1, m2, m3 of the 4 points and is updated in place.
+    auto field = [&](int f, int side, const CpmlC* cc, float2 ih, float2 ih2, const float* F0, const float* Fa,
+                     const float* Fd, float* mv) {
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+            const float2 f0 = pr(F0[2 * m], F0[2 * m + 1]), fa = pr(Fa[2 * m], Fa[2 * m + 1]),
+                         fd = pr(Fd[2 * m], Fd[2 * m + 1]);
+            const float2 gr = side ? psub(fa, fd) : psub(fd, fa);
+            const float2 lap = psub(padd(fd, fa), pmul(pr(2.0f, 2.0f), f0));
+            float2 m1 = pr(mv[2 * m], mv[2 * m + 1]);
+            float2 m2 = pr(mv[Q + 2 * m], mv[Q + 2 * m + 1]);
+            float2 m3 = pr(mv[2 * Q + 2 * m], mv[2 * Q + 2 * m + 1]);
+            const float2 o = cpml_mem2(cc[m], ih, ih2, gr, lap, m1, m2, m3);
+            if (f == 0) cu[m] = padd(cu[m], o); else if (f == 1) cv[m] = padd(cv[m], o); else cw[m] = padd(cw[m], o);
+            mv[2 * m] = m1.x; mv[2 * m + 1] = m1.y;
+            mv[Q + 2 * m] = m2.x; mv[Q + 2 * m + 1] = m2.y;
+            mv[2 * Q + 2 * m] = m3.x; mv[2 * Q + 2 * m + 1] = m3.y;
+        }
+    };
     // x direction: the whole column lies in the strip
     if (i < d || i >= nx - d) {
         const int side = i < d ? 0 : 1;
         const int kx = side ? i - (nx - d) : i;
         const float X = side ? float(kx + 1) * P.dx : float(d - i) * P.dx;
         const float inv_h = 1.0f / P.dx;
-        float c1[Q], c2[Q], c3[Q];
+        const float2 ih = pr(inv_h, inv_h), ih2 = pmul(ih, ih);
+        CpmlC cc[2];
 #pragma unroll
-        for (int k = 0; k < Q; ++k) cpml_c(P.kx, vel[k], X, P.dt, c1[k], c2[k], c3[k]);
+        for (int m = 0; m < 2; ++m) cc[m] = cpml_c2(P.kx, vel[m], pr(X, X), P.dt);
         const int vs = d * ld;
         const int off = ((side * 9) * d + kx) * ld + j;
         const float* rbase = rd.mx + off;
         float* wbase = wr.mx + off;
         // the next field's memory variables are loaded before this field's
         // stores (which the compiler must assume could alias them)
-        float nm[3][Q];
+        float nm[3 * Q];
 #pragma unroll
-        for (int v = 0; v < 3; ++v) ldv(rbase + v * vs, nm[v]);
+        for (int v = 0; v < 3; ++v) ldv(rbase + v * vs, &nm[v * Q]);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             float F0v[Q], Fav[Q], Fdv[Q];
@@ -417,31 +464,27 @@ __device__ __forceinline__ void cpml_vec(const PropDesc& P, const float* fbase, 
             ldv(col, F0v);
             ldv(col + BZ, Fav);
             ldv(col - BZ, Fdv);
-            float m1[Q], m2[Q], m3[Q];
+            float mv[3 * Q];
 #pragma unroll
-            for (int k = 0; k < Q; ++k) { m1[k] = nm[0][k]; m2[k] = nm[1][k]; m3[k] = nm[2][k]; }
+            for (int k = 0; k < 3 * Q; ++k) mv[k] = nm[k];
             if (f < 2) {
 #pragma unroll
-                for (int v = 0; v < 3; ++v) ldv(rbase + (f * 3 + 3 + v) * vs, nm[v]);
+                for (int v = 0; v < 3; ++v) ldv(rbase + (f * 3 + 3 + v) * vs, &nm[v * Q]);
             }
+            if (f == 0 && srcamp != 0.0f) {
 #pragma unroll
-            for (int k = 0; k < Q; ++k) {
-                float F0 = F0v[k], Fa = Fav[k], Fd = Fdv[k];
-                if (f == 0 && srcamp != 0.0f) {
-                    if (src == p + k) F0 -= srcamp;
-                    if (src == p + k + ld) Fa -= srcamp;
-                    if (src == p + k - ld) Fd -= srcamp;
+                for (int k = 0; k < Q; ++k) {
+                    if (src == p + k) F0v[k] -= srcamp;
+                    if (src == p + k + ld) Fav[k] -= srcamp;
+                    if (src == p + k - ld) Fdv[k] -= srcamp;
                 }
-                const float gr = side ? Fa - Fd : Fd - Fa;
-                const float lap = (Fd + Fa) - 2.0f * F0;
-                const float o = cpml_mem(c1[k], c2[k], c3[k], inv_h, gr, lap, m1[k], m2[k], m3[k]);
-                if (f == 0) cu[k] += o; else if (f == 1) cv[k] += o; else cw[k] += o;
             }
+            field(f, side, cc, ih, ih2, F0v, Fav, Fdv, mv);
             if (store) {
-                float* m = wbase + (f * 3) * vs;
-                stv(m, m1);
-                stv(m + vs, m2);
-                stv(m + 2 * vs, m3);
+                float* mw = wbase + (f * 3) * vs;
+                stv(mw, &mv[0]);
+                stv(mw + vs, &mv[Q]);
+                stv(mw + 2 * vs, &mv[2 * Q]);
             }
         }
     }
@@ -452,22 +495,25 @@ __device__ __forceinline__ void cpml_vec(const PropDesc& P, const float* fbase, 
         if (side == 0 ? !(j < d) : !(j + Q - 1 >= nz - d)) continue;
         const int k0 = side ? j - P.zb0 : j;
         const float inv_h = 1.0f / P.dz;
-        float c1[Q], c2[Q], c3[Q];
+        const float2 ih = pr(inv_h, inv_h), ih2 = pmul(ih, ih);
+        float X[Q];
 #pragma unroll
         for (int k = 0; k < Q; ++k) {
             const int jk = j + k;
-            float X = 0.0f;                                  // outside: c = (1, 0, 0)
-            if (side == 0 && jk < d) X = float(d - jk) * P.dz;
-            if (side == 1 && jk >= nz - d && jk < nz) X = float(jk - (nz - d) + 1) * P.dz;
-            cpml_c(P.kz, vel[k], X, P.dt, c1[k], c2[k], c3[k]);
+            X[k] = 0.0f;                                     // outside: c = (1, 0, 0)
+            if (side == 0 && jk < d) X[k] = float(d - jk) * P.dz;
+            if (side == 1 && jk >= nz - d && jk < nz) X[k] = float(jk - (nz - d) + 1) * P.dz;
         }
+        CpmlC cc[2];
+#pragma unroll
+        for (int m = 0; m < 2; ++m) cc[m] = cpml_c2(P.kz, vel[m], pr(X[2 * m], X[2 * m + 1]), P.dt);
         const int vs = nx * P.dpz;
         const int off = ((side * 9) * nx + i) * P.dpz + k0;
         const float* rbase = rd.mz + off;
         float* wbase = wr.mz + off;
-        float nm[3][Q];
+        float nm[3 * Q];
 #pragma unroll
-        for (int v = 0; v < 3; ++v) ldv(rbase + v * vs, nm[v]);
+        for (int v = 0; v < 3; ++v) ldv(rbase + v * vs, &nm[v * Q]);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const float* col = fbase + f * FS + c * BZ + r0;
@@ -475,31 +521,30 @@ __device__ __forceinline__ void cpml_vec(const PropDesc& P, const float* fbase, 
             Fc[0] = col[-1];
             ldv(col, &Fc[1]);
             Fc[Q + 1] = col[Q];
-            float m1[Q], m2[Q], m3[Q];
+            float mv[3 * Q];
 #pragma unroll
-            for (int k = 0; k < Q; ++k) { m1[k] = nm[0][k]; m2[k] = nm[1][k]; m3[k] = nm[2][k]; }
+            for (int k = 0; k < 3 * Q; ++k) mv[k] = nm[k];
             if (f < 2) {
 #pragma unroll
-                for (int v = 0; v < 3; ++v) ldv(rbase + (f * 3 + 3 + v) * vs, nm[v]);
+                for (int v = 0; v < 3; ++v) ldv(rbase + (f * 3 + 3 + v) * vs, &nm[v * Q]);
             }
+            float F0v[Q], Fav[Q], Fdv[Q];
 #pragma unroll
-            for (int k = 0; k < Q; ++k) {
-                float F0 = Fc[k + 1], Fa = Fc[k + 2], Fd = Fc[k];
-                if (f == 0 && srcamp != 0.0f) {
-                    if (src == p + k) F0 -= srcamp;
-                    if (src == p + k + 1) Fa -= srcamp;
-                    if (src == p + k - 1) Fd -= srcamp;
+            for (int k = 0; k < Q; ++k) { F0v[k] = Fc[k + 1]; Fav[k] = Fc[k + 2]; Fdv[k] = Fc[k]; }
+            if (f == 0 && srcamp != 0.0f) {
+#pragma unroll
+                for (int k = 0; k < Q; ++k) {
+                    if (src == p + k) F0v[k] -= srcamp;
+                    if (src == p + k + 1) Fav[k] -= srcamp;
+                    if (src == p + k - 1) Fdv[k] -= srcamp;
                 }
-                const float gr = side ? Fa - Fd : Fd - Fa;
-                const float lap = (Fd + Fa) - 2.0f * F0;
-                const float o = cpml_mem(c1[k], c2[k], c3[k], inv_h, gr, lap, m1[k], m2[k], m3[k]);
-                if (f == 0) cu[k] += o; else if (f == 1) cv[k] += o; else cw[k] += o;
             }
+            field(f, side, cc, ih, ih2, F0v, Fav, Fdv, mv);
             if (store) {
-                float* m = wbase + (f * 3) * vs;
-                stv(m, m1);
-                stv(m + vs, m2);
-                stv(m + 2 * vs, m3);
+                float* mw = wbase + (f * 3) * vs;
+                stv(mw, &mv[0]);
+                stv(mw + vs, &mv[Q]);
+                stv(mw + 2 * vs, &mv[2 * Q]);
             }
         }
     }

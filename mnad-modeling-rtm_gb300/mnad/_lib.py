@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libmnad.so")
 OK, E_ARG, E_OOM, E_CUDA, E_TIMEOUT, E_NOTFOUND, E_NUMERIC, E_BUDGET, E_STATE = range(9)
 SNAP_F32, SNAP_BF16, SNAP_F16 = 0, 1, 2
 PAIR_REFERENCE, PAIR_ALIGNED = 0, 1
-KERNEL_AUTO, KERNEL_DIRECT, KERNEL_TMA, KERNEL_TUNE, KERNEL_TMA2 = 0, 1, 2, 3, 4
+KERNEL_AUTO, KERNEL_DIRECT, KERNEL_TMA, KERNEL_TUNE, KERNEL_TMA2, KERNEL_TMA_NARROW = 0, 1, 2, 3, 4, 5
 JOB_MODEL, JOB_RTM = 0, 1
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 

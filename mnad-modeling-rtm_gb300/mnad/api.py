@@ -20,7 +20,7 @@ from ._lib import Job, MnadError, Options, check, lib
 _CODECS = {"f32": _lib.SNAP_F32, "bf16": _lib.SNAP_BF16, "f16": _lib.SNAP_F16}
 _PAIRINGS = {"reference": _lib.PAIR_REFERENCE, "aligned": _lib.PAIR_ALIGNED}
 _KERNELS = {"auto": _lib.KERNEL_AUTO, "direct": _lib.KERNEL_DIRECT, "tma": _lib.KERNEL_TMA,
-            "tune": _lib.KERNEL_TUNE, "tma2": _lib.KERNEL_TMA2}
+            "tune": _lib.KERNEL_TUNE, "tma2": _lib.KERNEL_TMA2, "tma_narrow": _lib.KERNEL_TMA_NARROW}
 
 
 def _f64(a, order="F"):

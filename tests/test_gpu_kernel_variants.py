@@ -1,14 +1,16 @@
-"""The two-step kernel (temporal blocking of depth 2, MNAD_KERNEL_TMA2).
+"""The variants of the persistent kernel: two steps per pass (temporal
+blocking of depth 2, MNAD_KERNEL_TMA2) and 64 x 8 tiles (MNAD_KERNEL_TMA_NARROW).
 
-Per point it runs the arithmetic of the one-step persistent kernel, so its
+Per point both run the arithmetic of the one-step 64 x 16 kernel, so their
 outputs must equal that kernel's exactly, for every event the reference's time
 loop has (SRC/MNAD/fwd_PDE_exact_MNAD.m:92-157, SRC/migration/Born_adj_MNAD.m:
 85-136): CPML strips on all sides and in corners, a source inside a strip and
-on tile edges, receivers on tile edges (the adjoint injects them in the ring
-a pass computes around its tile), snapshots on either sub-step (odd T), the
-tt = 1, 2 snapshot formulas, odd record lengths (the last pass runs one step),
-no CPML, several grids and record lengths in one plan.  One RTM shot is also
-checked against the FP64 oracle.
+on tile edges, receivers on tile edges (the two-step kernel's adjoint injects
+them in the ring a pass computes around its tile; the narrow kernel reads half
+of a receiver bucket), snapshots on either sub-step (odd T), the tt = 1, 2
+snapshot formulas, odd record lengths (the two-step kernel's last pass runs one
+step), no CPML, several grids and record lengths in one plan.  One RTM shot per
+variant is also checked against the FP64 oracle.
 """
 import numpy as np
 import pytest
@@ -64,12 +66,17 @@ def fwd(kernel, s, indx=0, ss=1, codec="f32", T=0, ctx=None):
             ctx.close()
 
 
+VARIANTS = ["tma2", "tma_narrow"]
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("geom", [dict(), dict(nt=300), dict(zs=64, xs=16), dict(zs=1, xs=1), dict(zs=150, xs=100),
-                                  dict(d=0), dict(nz=64, nx=16, d=6, nt=120, xs=9), dict(nz=200, nx=97, d=40)])
-def test_forward_equals_the_one_step_kernel(geom):
+                                  dict(d=0), dict(nz=64, nx=16, d=6, nt=120, xs=9), dict(nz=200, nx=97, d=40),
+                                  dict(xs=8), dict(xs=9)])
+def test_forward_equals_the_one_step_kernel(geom, variant):
     s = shot(**geom)
     a = fwd("tma", s)
-    b = fwd("tma2", s)
+    b = fwd(variant, s)
     for x, y, name in zip(a, b, ("U", "V", "W")):
         assert np.linalg.norm(x) > 0
         assert np.array_equal(x, y), f"{name} traces differ ({geom}): rel {rel(y, x):.2e}"
@@ -86,23 +93,25 @@ def rtm(kernel, s, codec, T):
     return d_true, d_bg, UU, illum, im
 
 
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("codec,T", [("f32", 3), ("bf16", 4), ("f32", 1)])
-def test_rtm_equals_the_one_step_kernel(codec, T):
+def test_rtm_equals_the_one_step_kernel(codec, T, variant):
     """Snapshots and imaging on both sub-steps (odd T), at every step (T = 1:
     the tt = 1 and 2 formulas), and the adjoint's injection of receivers on
     tile edges and inside the top strip."""
     s = shot(nt=241)
     a = rtm("tma", s, codec, T)
-    b = rtm("tma2", s, codec, T)
+    b = rtm(variant, s, codec, T)
     for x, y, name in zip(a, b, ("gather", "background gather", "UU", "illum", "image")):
         assert np.linalg.norm(x) > 0, name
         assert np.array_equal(x, y), f"{name} differs ({codec}, T={T}): rel {rel(y, x):.2e}"
 
 
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("nt", [1, 2, 3])
-def test_shortest_records(nt):
+def test_shortest_records(nt, variant):
     s = shot(nt=nt)
-    for x, y in zip(rtm("tma", s, "f32", 1), rtm("tma2", s, "f32", 1)):
+    for x, y in zip(rtm("tma", s, "f32", 1), rtm(variant, s, "f32", 1)):
         assert np.array_equal(x, y)
 
 
@@ -128,10 +137,12 @@ def _plan(kernel):
     return jobs, launches
 
 
-def test_plan_of_mixed_grids_and_lengths_equals_the_one_step_kernel():
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_plan_of_mixed_grids_and_lengths_equals_the_one_step_kernel(variant):
     a, la = _plan("tma")
-    b, lb = _plan("tma2")
-    assert lb < la                          # the two-step kernel ran: one launch per two steps
+    b, lb = _plan(variant)
+    if variant == "tma2":
+        assert lb < la                      # the two-step kernel ran: one launch per two steps
     for ja, jb in zip(a, b):
         assert np.array_equal(ja.data, jb.data)
         if ja.kind == "rtm":
@@ -140,7 +151,8 @@ def test_plan_of_mixed_grids_and_lengths_equals_the_one_step_kernel():
             assert np.array_equal(ja.illum, jb.illum)
 
 
-def test_rtm_shot_against_the_oracle():
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_rtm_shot_against_the_oracle(variant):
     s = shot(nz=181, nx=241, d=20, nt=600, zs=21, xs=121)
     T = 4
     nf = P.snapshot_nf(s["vs"], s["nt"])
@@ -150,9 +162,9 @@ def test_rtm_shot_against_the_oracle():
     bg = coracle.fwd(*a, s["vs"], s["dt"], s["nt"], s["w"], s["d"], indx=1, T=T, ncols=ncols)
     im = coracle.adj(s["dx"], s["dz"], s["nt"], s["dt"], s["vs"], s["xr"], s["zr"], data - bg["datau"], s["d"],
                      bg["UU"], T)
-    g, gb, UU, illum, img = rtm("tma2", s, "f32", T)
+    g, gb, UU, illum, img = rtm(variant, s, "f32", T)
     errs = dict(gather=rel(g, data), gather_bg=rel(gb, bg["datau"]), illum=rel(illum, bg["illum"]),
                 image=rel(img, im))
-    print("two-step kernel vs FP64 oracle: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+    print(f"{variant} kernel vs FP64 oracle: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
     assert errs["gather"] <= TOL_GATHER and errs["gather_bg"] <= TOL_GATHER
     assert errs["illum"] <= TOL_IMAGE and errs["image"] <= TOL_IMAGE

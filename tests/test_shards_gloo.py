@@ -45,11 +45,11 @@ def _shot_stack(sv, xs):
     return T * im.reshape(shape, order="F"), T * bg["illum"]
 
 
-def _worker(rank, world, port, fail_rank, q):
+def _worker(rank, world, port, fail_rank, q, timeout_s):
     import torch.distributed as dist
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     import datetime
-    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=8))
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=timeout_s))
     try:
         sv = _survey()
         mine = shards.shard(sv["shots"], rank, world)
@@ -69,11 +69,14 @@ def _worker(rank, world, port, fail_rank, q):
             pass
 
 
-def _run(world, fail_rank=-1):
+def _run(world, fail_rank=-1, timeout_s=60):
+    """Run the ranks; `timeout_s` bounds every collective (a generous bound
+    when all ranks are healthy -- their oracle shots may run on a loaded host --
+    and a short one where a failed rank must be detected)."""
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_worker, args=(r, world, port, fail_rank, q)) for r in range(world)]
+    procs = [ctx.Process(target=_worker, args=(r, world, port, fail_rank, q, timeout_s)) for r in range(world)]
     for p in procs:
         p.start()
     res = {}
@@ -113,6 +116,6 @@ def test_two_gloo_ranks_reduce_to_the_single_process_stack():
 
 
 def test_a_failed_rank_makes_the_reduction_fail_not_hang():
-    res = _run(2, fail_rank=1)
+    res = _run(2, fail_rank=1, timeout_s=8)
     assert res[1][0] == "error"
     assert res[0][0] == "error"          # the surviving rank's collective errors out (timeout or peer loss)
