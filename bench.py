@@ -372,6 +372,7 @@ def run_ours(args):
     clocks = sampler.stop()
     status = ctx.status()
     pts, abytes = plan.work()
+    kernels = plan.kernels()     # step kernel of each phase (the tuner's choice under --kernel tune)
     total_s = allmax(sum(run_ms) / 1e3, world)
     pts_all = allsum(pts * args.steps, world)
     value = pts_all / total_s / 1e9
@@ -386,8 +387,8 @@ def run_ours(args):
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
             "peak_kind": f"{peak_kind} hbm_gbs",
-            "kernel": {"direct": "mnad::step_direct", "tma2": "mnad::step_tma2",
-                       "tma_narrow": "mnad::step_tma_narrow"}.get(args.kernel, "mnad::step_tma"),
+            "kernel": "mnad::step_" + (kernels["forward"] or "tma"),
+            "kernels_by_phase": kernels,
             "algorithmic_bytes_per_launch": abytes / plan.timing()["step_launches"]}
     # the same roofline split by phase (forwards with snapshots; adjoints with imaging)
     ph = plan.phases()

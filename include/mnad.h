@@ -63,9 +63,11 @@ enum { MNAD_SNAP_F32 = 0, MNAD_SNAP_BF16 = 1, MNAD_SNAP_F16 = 2 };
 enum { MNAD_PAIR_REFERENCE = 0, MNAD_PAIR_ALIGNED = 1 };
 
 /* Step kernel choice.  AUTO picks per launch group (propagations of one grid
- * size advancing together): the persistent TMA kernel (64 x 16 tiles) once a
- * launch has about 2.25 of its tiles per resident CTA (0.7M point-updates on
- * a 152-SM GB300), the one-thread-per-point kernel (32 x 8 tiles) below.
+ * size advancing together): the persistent TMA kernel once a launch has about
+ * 2.25 of its 64 x 16 tiles per resident CTA (0.7M point-updates on a 152-SM
+ * GB300) -- on 64 x 8 tiles (TMA_NARROW) where the CPML strips hold under
+ * 15 % of the grid's points, on 64 x 16 tiles otherwise -- and the
+ * one-thread-per-point kernel (32 x 8 tiles) below.
  * TMA_NARROW is the persistent kernel on 64 x 8 tiles (128 threads per CTA,
  * 4 CTAs per SM); its outputs are bitwise those of TMA.
  * TMA2 is the persistent kernel advancing two time steps per pass (temporal
@@ -271,6 +273,11 @@ MNAD_API int mnad_plan_timing(const mnad_plan* plan, double* run_ms, double* ste
  * phase also holds the background recomputation). */
 MNAD_API int mnad_plan_phases(const mnad_plan* plan, double* forward_ms, double* forward_bytes, double* adjoint_ms,
                               double* adjoint_bytes);
+/* Step kernel (MNAD_KERNEL_DIRECT, _TMA, _TMA_NARROW or _TMA2) that the
+ * forward phase and the adjoint phase of the plan run, for the launch group
+ * with the most tiles (after MNAD_KERNEL_TUNE's trials, once the plan has
+ * run).  -1 where a phase has no propagation. */
+MNAD_API int mnad_plan_kernels(const mnad_plan* plan, int* forward_kernel, int* adjoint_kernel);
 /* Stack of the plan's RTM shots after mnad_plan_run, formed in FP64 on the
  * device (SRC/migration/main_Acoustic_RTM.m:237-262): image_sum = sum of the
  * shots' images (each T*sum US.*UR), illum_sum = sum of the shots'

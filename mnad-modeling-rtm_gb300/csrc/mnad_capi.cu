@@ -427,6 +427,10 @@ struct mnad_plan {
     double bytes_fwd = 0, bytes_adj = 0;        // phase 1 / phase 3 (with the recomputation)
     float run_ms = 0, step_ms = 0, fwd_ms = 0, adj_ms = 0;
     int launches = 0;
+    // run once and destroyed (mnad_run_jobs): launch the steps directly --
+    // capturing and instantiating a graph of thousands of launches costs more
+    // than it saves on a single run, and direct launches overlap the GPU work
+    bool once = false;
     ~mnad_plan()
     {
         if (ctx) cudaStreamSynchronize(ctx->stream);
@@ -619,7 +623,7 @@ MNAD_API int mnad_plan_run(mnad_plan* P)
         need(P != nullptr, "plan is NULL");
         Context& c = *P->ctx;
         MNAD_CK(cudaSetDevice(c.device));
-        const bool g = c.opt.use_graphs != 0;
+        const bool g = c.opt.use_graphs != 0 && !P->once;
         MNAD_CK(cudaEventRecord(P->ev[0], c.stream));
         P->phase1->run(g);
         MNAD_CK(cudaEventRecord(P->ev[1], c.stream));
@@ -724,6 +728,15 @@ MNAD_API int mnad_plan_phases(const mnad_plan* P, double* forward_ms, double* fo
     });
 }
 
+MNAD_API int mnad_plan_kernels(const mnad_plan* P, int* forward_kernel, int* adjoint_kernel)
+{
+    return guard([&] {
+        need(P != nullptr, "plan is NULL");
+        if (forward_kernel) *forward_kernel = P->phase1->main_kind();
+        if (adjoint_kernel) *adjoint_kernel = P->phase3->main_kind();
+    });
+}
+
 MNAD_API int mnad_plan_stack(mnad_plan* P, double* image_sum, double* illum_sum, double* img_rtm)
 {
     return guard([&] {
@@ -763,6 +776,7 @@ MNAD_API int mnad_run_jobs(mnad_context* ctx, const mnad_job* jobs, int njobs)
     mnad_plan* P = nullptr;
     int rc = mnad_plan_create(ctx, jobs, njobs, &P);
     if (rc != MNAD_OK) return rc;
+    P->once = true;
     rc = mnad_plan_run(P);
     if (rc == MNAD_OK) rc = mnad_plan_download(P);
     const std::string keep = last_error();

@@ -700,13 +700,33 @@ int Batch::pick_kind(const LaunchGroup& g) const
     if (tc_.kind == MNAD_KERNEL_DIRECT || tc_.kind == MNAD_KERNEL_TMA || tc_.kind == MNAD_KERNEL_TMA2 ||
         tc_.kind == MNAD_KERNEL_TMA_NARROW)
         return valid(tc_.kind);
+    const double tiles = (double)g.props.size() * ((g.nz + TMA_TZ - 1) / TMA_TZ) * ((g.nx + TMA_TX - 1) / TMA_TX);
+    const bool persistent = tiles >= AUTO_TMA_TILES_PER_CTA * ctx_.num_sms * TMA_CTAS_PER_SM;
     if (tc_.kind == MNAD_KERNEL_TUNE) {
         if (trial_kind_ >= 0) return valid(trial_kind_);
         auto it = ctx_.kernel_choice.find(std::make_tuple(g.nz, g.nx, g.d, (int)g.props.size()));
         if (it != ctx_.kernel_choice.end()) return valid(it->second);
+        // a group that was not measured itself (the step windows of a
+        // checkpointed adjoint leave no room for trial steps): the choice
+        // measured on the same grid with the nearest propagation count, if
+        // both launches are large enough for the persistent kernels
+        int best = -1, gap = INT_MAX;
+        for (const auto& kv : ctx_.kernel_choice) {
+            const auto& key = kv.first;
+            if (std::get<0>(key) != g.nz || std::get<1>(key) != g.nx || std::get<2>(key) != g.d) continue;
+            const int dg = std::abs(std::get<3>(key) - (int)g.props.size());
+            if (dg < gap && kv.second != MNAD_KERNEL_DIRECT) best = kv.second, gap = dg;
+        }
+        if (best >= 0 && persistent) return valid(best);
     }
-    const double tiles = (double)g.props.size() * ((g.nz + TMA_TZ - 1) / TMA_TZ) * ((g.nx + TMA_TX - 1) / TMA_TX);
-    return tiles >= AUTO_TMA_TILES_PER_CTA * ctx_.num_sms * TMA_CTAS_PER_SM ? MNAD_KERNEL_TMA : MNAD_KERNEL_DIRECT;
+    if (!persistent) return MNAD_KERNEL_DIRECT;
+    // Tile width: the narrow tiles win where the CPML strips are a small share
+    // of the grid, the 64 x 16 tiles where they are large (measured on GB300:
+    // strips 8 % of the 1281 x 4081 grid, narrow +3.8 %; 22 % of 481 x 1281,
+    // narrow -2.6 %).
+    const double inner = (double)std::max(0, g.nz - 2 * g.d) * std::max(0, g.nx - 2 * g.d);
+    const double strip_share = 1.0 - inner / ((double)g.nz * g.nx);
+    return strip_share < AUTO_NARROW_STRIP_SHARE ? MNAD_KERNEL_TMA_NARROW : MNAD_KERNEL_TMA;
 }
 
 void Batch::tune()
@@ -936,6 +956,17 @@ int Batch::step_launches() const
     for (const auto& g : groups_)
         if (g->ntiles > 0) n += g->kind == MNAD_KERNEL_TMA2 ? (nsteps_ + 1) / 2 : nsteps_;
     return n;
+}
+
+int Batch::main_kind() const
+{
+    int kind = -1, most = 0;
+    for (const auto& g : groups_)
+        if (g->ntiles > most) {
+            most = g->ntiles;
+            kind = g->kind;
+        }
+    return kind;
 }
 
 int Batch::group_kind_count(int kind) const

@@ -95,6 +95,10 @@ TileCfg tile_cfg(int kernel);
 // the persistent TMA kernel from 0.82M (800 tiles, 2.6 per CTA) on; its
 // pipeline needs a few tiles per CTA to hide the load latency.
 constexpr double AUTO_TMA_TILES_PER_CTA = 2.25;
+// AUTO: the narrow (64 x 8) tiles below this share of CPML strip points in
+// the grid, the 64 x 16 tiles above it (between two measured grids: 8 % and
+// 22 %).
+constexpr double AUTO_NARROW_STRIP_SHARE = 0.15;
 constexpr int TUNE_WARMUP = 2, TUNE_STEPS = 8;
 
 // Receivers of one propagation bucketed by TMA_TZ x TMA_TX tile and, within a
@@ -205,6 +209,7 @@ public:
     int launches_per_step() const;     // step-kernel launches of one time step
     int step_launches() const;         // step-kernel launches of a whole run (run())
     int group_kind_count(int kind) const;   // launch groups running that kernel
+    int main_kind() const;             // kernel of the group with the most tiles (-1: no group)
     int group_kind(size_t g) const { return groups_[g]->kind; }
     size_t groups() const { return groups_.size(); }
     int steps() const { return nsteps_; }

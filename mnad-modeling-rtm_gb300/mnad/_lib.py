@@ -90,6 +90,7 @@ SIGNATURES = {
     "mnad_plan_work": ([_vp, _dp, _dp], C.c_int),
     "mnad_plan_timing": ([_vp, _dp, _dp, C.POINTER(C.c_int)], C.c_int),
     "mnad_plan_phases": ([_vp, _dp, _dp, _dp, _dp], C.c_int),
+    "mnad_plan_kernels": ([_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
     "mnad_plan_stack": ([_vp, _dp, _dp, _dp], C.c_int),
     "mnad_server_create": ([C.c_int, C.POINTER(ServerOptions), C.POINTER(_vp)], C.c_int),
     "mnad_server_submit": ([_vp, C.POINTER(Job), C.POINTER(C.c_uint64)], C.c_int),

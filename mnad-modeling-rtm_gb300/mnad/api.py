@@ -321,6 +321,14 @@ class Plan:
         return {"forward_ms": v[0].value, "forward_bytes": v[1].value, "adjoint_ms": v[2].value,
                 "adjoint_bytes": v[3].value}
 
+    def kernels(self):
+        """{'forward': name, 'adjoint': name} of the step kernels the phases run
+        (the largest launch group of each; None where a phase is empty)."""
+        f, a = C.c_int(), C.c_int()
+        check(lib().mnad_plan_kernels(self._h, C.byref(f), C.byref(a)))
+        names = {v: k for k, v in _KERNELS.items()}
+        return {"forward": names.get(f.value), "adjoint": names.get(a.value)}
+
     def stack(self):
         """(image_sum, illum_sum, img_rtm) of the RTM shots, (nz-2d, nx-2d) arrays."""
         rtm = [j for j in self.jobs if j.kind == "rtm"]
