@@ -20,6 +20,32 @@ from .api import Context
 
 _default_ctx = None
 
+# A MAT v5 data element stores its size in 32 bits and MATLAB reads variables
+# of at most 2 GiB from such files; larger ones need the HDF5-based v7.3
+# format, which this module does not write.
+MAT_V5_MAX_BYTES = 2 ** 31 - 1
+
+
+def _payload_bytes(x) -> int:
+    if isinstance(x, dict):
+        return sum(_payload_bytes(v) for v in x.values())
+    a = np.asarray(x)
+    if a.dtype == object:
+        return sum(_payload_bytes(v) for v in a.ravel())
+    return a.nbytes
+
+
+def _savemat(path: str, variables: dict):
+    """scipy.io.savemat in MAT v5, refusing variables MATLAB could not read
+    back (over 2 GiB) instead of writing a broken file."""
+    import scipy.io
+    for name, val in variables.items():
+        n = _payload_bytes(val)
+        if n > MAT_V5_MAX_BYTES:
+            raise ValueError(f"variable '{name}' holds {n} bytes: MAT v5 files keep at most {MAT_V5_MAX_BYTES} "
+                             "bytes per variable; keep it on the device (mnad_wavefield_*) or write it in parts")
+    scipy.io.savemat(path, variables, format="5")
+
 
 def default_context() -> Context:
     global _default_ctx
@@ -60,13 +86,16 @@ def Born_adj_MNAD(dx, dz, nt, dt, v, xr, zr, data, d_pml, ss,
 def save_wavefield(ctx: Context, ss: int, nz: int, nx: int, d_pml: int, directory: str = "."):
     """Write ``Wavefields/UU_<ss>.mat`` and ``Illuminations/illum_<ss>.mat``
     (variables ``UU`` and ``illum``) as ``fwd_PDE_exact_MNAD.m:160-164`` does."""
-    import scipy.io
+    info = ctx.wavefield_info(ss)
+    if info["nint"] * info["ncols"] * 8 > MAT_V5_MAX_BYTES:
+        raise ValueError(f"UU of shot {ss} holds {info['nint'] * info['ncols'] * 8} bytes: MAT v5 files keep at most "
+                         f"{MAT_V5_MAX_BYTES} bytes per variable; keep it on the device (mnad_wavefield_*)")
     UU, illum = ctx.wavefield_export(ss)
     os.makedirs(os.path.join(directory, "Wavefields"), exist_ok=True)
     os.makedirs(os.path.join(directory, "Illuminations"), exist_ok=True)
-    scipy.io.savemat(os.path.join(directory, "Wavefields", f"UU_{ss}.mat"), {"UU": UU})
-    scipy.io.savemat(os.path.join(directory, "Illuminations", f"illum_{ss}.mat"),
-                     {"illum": illum.reshape((nz - 2 * d_pml, nx - 2 * d_pml), order="F")})
+    _savemat(os.path.join(directory, "Wavefields", f"UU_{ss}.mat"), {"UU": UU})
+    _savemat(os.path.join(directory, "Illuminations", f"illum_{ss}.mat"),
+             {"illum": illum.reshape((nz - 2 * d_pml, nx - 2 * d_pml), order="F")})
 
 
 def load_wavefield(ctx: Context, ss: int, nz: int, nx: int, d_pml: int, nt: int, T: int, directory: str = "."):
@@ -110,18 +139,16 @@ def save_data(path: str, data, profile: dict):
     main_Acoustic_Data.m:179): ``data`` is the 1 x ns cell of the forward's
     returns, each the 1 x 1 cell ``{datau}``; pass the per-shot ``datau``
     (nt x nr) arrays or the one-element lists ``fwd_PDE_exact_MNAD`` returns."""
-    import scipy.io
     shots = [d[0] if isinstance(d, (list, tuple)) else d for d in data]
-    scipy.io.savemat(path, {"data": _cell_row([_cell_row([np.asarray(d, dtype=np.float64)]) for d in shots]),
-                            "profile": {k: profile[k] for k in PROFILE_FIELDS}}, format="5")
+    _savemat(path, {"data": _cell_row([_cell_row([np.asarray(d, dtype=np.float64)]) for d in shots]),
+                    "profile": {k: profile[k] for k in PROFILE_FIELDS}})
 
 
 def save_scattered(path: str, data_sct, profile: dict):
     """``save data_scattered_MNAD_Acoustic data_sct profile``
     (main_Acoustic_RTM.m:234): the 1 x ns cell of scattered gathers."""
-    import scipy.io
-    scipy.io.savemat(path, {"data_sct": _cell_row([np.asarray(d, dtype=np.float64) for d in data_sct]),
-                            "profile": {k: profile[k] for k in PROFILE_FIELDS}}, format="5")
+    _savemat(path, {"data_sct": _cell_row([np.asarray(d, dtype=np.float64) for d in data_sct]),
+                    "profile": {k: profile[k] for k in PROFILE_FIELDS}})
 
 
 def load_data(path: str):
@@ -138,5 +165,4 @@ def load_data(path: str):
 def save_illum_average(path: str, illum):
     """``save(['./Illuminations/illum_' num2str(0)],'illum')``
     (main_Acoustic_RTM.m:237-244): the illumination averaged over the shots."""
-    import scipy.io
-    scipy.io.savemat(path, {"illum": np.asarray(illum, dtype=np.float64)}, format="5")
+    _savemat(path, {"illum": np.asarray(illum, dtype=np.float64)})

@@ -52,3 +52,15 @@ def test_scattered_file_and_illumination(tmp_path):
     q = str(tmp_path / "illum_0.mat")
     R.save_illum_average(q, il)
     assert np.array_equal(scipy.io.loadmat(q)["illum"], il)
+
+
+def test_writers_refuse_variables_matlab_could_not_read(tmp_path, monkeypatch):
+    """MAT v5 keeps at most 2 GiB per variable: a larger one is refused with a
+    clear error rather than written into a file MATLAB's load rejects (the
+    limit is lowered here so the test needs no 2 GiB array)."""
+    import pytest
+    monkeypatch.setattr(R, "MAT_V5_MAX_BYTES", 1000)
+    g = _gathers(2, nt=50, nr=7)                  # 2 x 2800 bytes
+    with pytest.raises(ValueError, match="at most 1000 bytes"):
+        R.save_scattered(str(tmp_path / "big.mat"), g, _profile(2))
+    R.save_illum_average(str(tmp_path / "small.mat"), np.ones((10, 10)))   # 800 bytes: written
