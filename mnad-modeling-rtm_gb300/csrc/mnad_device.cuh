@@ -296,4 +296,34 @@ __device__ __forceinline__ float snap_decode(const void* base, int codec, size_t
     return static_cast<const float*>(base)[i];
 }
 
+// The FP64 value of a float, from its IEEE-754 fields with integer
+// operations: sign, exponent rebiased from 127 to 1023 (+896), the 23
+// mantissa bits shifted to the top of the 52.  Exact for every normal float
+// and for zeros; subnormals, infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ double widen_f32(float x)
+{
+    const unsigned u = __float_as_uint(x);
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sign);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    const unsigned long long bits = sign | ((unsigned long long)(e + 896u) << 52) |
+                                    ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
+// acc += a * b for the FP64 illumination and image accumulations
+// (fwd_PDE_exact_MNAD.m:126-143, Born_adj_MNAD.m:127-134): the product is
+// formed in FP32 (one rounding, 2^-24 relative) and added in FP64, so a point
+// costs one FP64 operation -- GB300 runs FP64 at a small fraction of its FP32
+// rate -- instead of two conversions and an FP64 fused multiply-add.  A zero
+// product (the wave has not reached the point) leaves the accumulator, and its
+// memory, untouched.
+__device__ __forceinline__ void accumulate_product(double* acc, float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    if (p == 0.0f) return;
+    *acc += widen_f32(p);
+}
+
 }  // namespace mnad

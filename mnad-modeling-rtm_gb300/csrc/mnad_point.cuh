@@ -148,7 +148,7 @@ __device__ __forceinline__ void finish_point(const PropDesc& P, int tt, int j, i
                 if (P.codec == CODEC_BF16) static_cast<__nv_bfloat16*>(P.snap)[o] = __float2bfloat16_rn(d2u);
                 else static_cast<float*>(P.snap)[o] = d2u;   // FP32, or the FP16 codec's staging slot
             }
-            if (P.snap_flags & SNAP_ILLUM) P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
+            if (P.snap_flags & SNAP_ILLUM) accumulate_product(&P.illum[q], d2u, d2u);
         }
         if ((long long)p == P.src && tt < P.nt) xu += P.src_amp[tt];   // next step's injection
     } else {
@@ -165,7 +165,7 @@ __device__ __forceinline__ void finish_point(const PropDesc& P, int tt, int j, i
                 const size_t nint = (size_t)niz * (P.nx - 2 * d);
                 const float sc = P.codec == CODEC_F16 ? P.snap_scale[col - 1] : 1.0f;
                 const float us = snap_decode(P.snap, P.codec, (size_t)slot * nint + q, sc);
-                P.image[q] = fma((double)us, (double)xu, P.image[q]);
+                accumulate_product(&P.image[q], us, xu);
             }
         }
     }

@@ -13,7 +13,7 @@
 // descriptor and the tile's metadata.  Consumers (all TMA_THREADS threads,
 // thread 0 included) wait on that stage's "full" barrier, compute the tile
 // (each thread TMA_PZ consecutive z points of one column, a register window
-// along z; a warp covers 32 x TMA_PZ rows of one column) and write nU, nV, nW
+// along z; a warp covers two columns of TMA_TZ rows) and write nU, nV, nW
 // with vector stores over pU, pV, pW; each warp then
 // arrives on the stage's "empty" barrier.  Only the producer waits for
 // "empty" before refilling the stage, so no global-memory latency and no
@@ -230,8 +230,7 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
                     }
                     if (P.snap_flags & SNAP_ILLUM) {
 #pragma unroll
-                        for (int k = 0; k < Q; ++k)
-                            P.illum[q0 + k] = fma((double)d2u[k], (double)d2u[k], P.illum[q0 + k]);
+                        for (int k = 0; k < Q; ++k) accumulate_product(&P.illum[q0 + k], d2u[k], d2u[k]);
                     }
                 } else {
                     // Born_adj_MNAD.m:127-134
@@ -243,7 +242,7 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
 #pragma unroll
                         for (int k = 0; k < Q; ++k) {
                             const float us = snap_decode(P.snap, P.codec, o + k, sc);
-                            P.image[q0 + k] = fma((double)us, (double)ou[k], P.image[q0 + k]);
+                            accumulate_product(&P.image[q0 + k], us, ou[k]);
                         }
                     }
                 }
@@ -330,7 +329,7 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
                                 static_cast<__nv_bfloat16*>(P.snap)[o] = __float2bfloat16_rn(d2u);
                             else static_cast<float*>(P.snap)[o] = d2u;
                         }
-                        if (P.snap_flags & SNAP_ILLUM) P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
+                        if (P.snap_flags & SNAP_ILLUM) accumulate_product(&P.illum[q], d2u, d2u);
                     }
                 }
                 if (src_next != 0.0f) {
@@ -355,7 +354,7 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
                         const size_t q = (size_t)(q0 + k);
                         const float sc = P.codec == CODEC_F16 ? P.snap_scale[col - 1] : 1.0f;
                         const float us = snap_decode(P.snap, P.codec, (size_t)(col - 1 - P.snap_col0) * nint + q, sc);
-                        P.image[q] = fma((double)us, (double)ou[k], P.image[q]);
+                        accumulate_product(&P.image[q], us, ou[k]);
                     }
                 }
             }

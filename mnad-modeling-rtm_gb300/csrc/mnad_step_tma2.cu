@@ -176,7 +176,7 @@ __device__ __forceinline__ void quad_step(const StepArgs& A, const PropDesc& P, 
                     if (P.codec == CODEC_BF16) static_cast<__nv_bfloat16*>(P.snap)[o] = __float2bfloat16_rn(d2u);
                     else static_cast<float*>(P.snap)[o] = d2u;
                 }
-                if (P.snap_flags & SNAP_ILLUM) P.illum[q] = fma((double)d2u, (double)d2u, P.illum[q]);
+                if (P.snap_flags & SNAP_ILLUM) accumulate_product(&P.illum[q], d2u, d2u);
             }
         }
         // the next step's injection (fwd_PDE_exact_MNAD.m:111): stored U holds it
@@ -209,7 +209,7 @@ __device__ __forceinline__ void quad_step(const StepArgs& A, const PropDesc& P, 
                     if (!(jk >= d && jk < nz - d && i >= d && i < nx - d)) continue;
                     const size_t q = (size_t)(q0 + k);
                     const float us = snap_decode(P.snap, P.codec, o + q, sc);
-                    P.image[q] = fma((double)us, (double)ou[k], P.image[q]);
+                    accumulate_product(&P.image[q], us, ou[k]);
                 }
             }
         }
