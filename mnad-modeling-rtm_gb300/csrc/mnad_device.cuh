@@ -159,7 +159,7 @@ struct StepArgs {
     int tiles_per_prop;    // ntz * ntx (one geometry per launch group)
     int s;                 // global step index
     unsigned* status;      // launch-wide status word (ST_TIMEOUT: the launch did not finish its tiles)
-    unsigned spin_limit;   // polls of a bounded barrier wait before it gives up (TMA kernel)
+    unsigned spin_limit;   // polls of a bounded barrier wait before it gives up (persistent kernels; set by the host, > 0)
 };
 
 // Neighbourhood of one point for the three fields.  Naming: <f><z><x> with

@@ -821,7 +821,7 @@ void Batch::launch_group(size_t gi, int s, int slot)
         a.tiles_per_prop = g->tiles_per_prop;
         a.s = s;
         a.status = ctx_.d_status;
-        a.spin_limit = ctx_.wait_limit;
+        a.spin_limit = ctx_.wait_limit ? ctx_.wait_limit : SPIN_LIMIT_DEFAULT;
         const int grid = std::min(g->ntiles, ctx_.num_sms * TMA_CTAS_PER_SM);
         if (g->kind == MNAD_KERNEL_TMA)
             step_tma<<<grid, TMA_THREADS, step_tma_smem_bytes(), ctx_.stream>>>(a);

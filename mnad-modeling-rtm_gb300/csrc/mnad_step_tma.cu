@@ -114,14 +114,10 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
         return;
     }
     const int cur = A.s & 1;
-    const unsigned limit = A.spin_limit ? A.spin_limit : SPIN_LIMIT_DEFAULT;
     int next_claim = -1;                    // producer: tile claimed one refill ahead
-    // producer: operations that complete a phase of each stage's full barrier
-    // (a tile's copies, or the arrive of "no tile"); the last of them is the
-    // only one that can still be in flight
-    unsigned fills[NST];
-#pragma unroll
-    for (int k = 0; k < NST; ++k) fills[k] = 0;
+    // producer: operations issued that complete a phase of a full barrier (a
+    // tile's copies, or the arrive of "no tile"); fill f goes to stage f % NST
+    unsigned nfills = 0;
     if (tid == 0) {
         for (int k = 0; k < NST; ++k) {
             mbar_init(&full[k], 1);
@@ -141,7 +137,7 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
         for (int k = 0; k < NST; ++k) {
             if (stage_tile[k] >= 0) issue_tile<TX>(A, stage_tile[k], stages[k], &full[k], cur);
             else mbar_arrive(&full[k]);     // releases the consumers: no tile
-            fills[k] = 1;
+            ++nfills;
         }
     const int tzt = tid % TMA_TZY, txt = tid / TMA_TZY;
     const int c = txt + 2, r0 = tzt * TMA_PZ + 4;
@@ -152,7 +148,7 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
         const unsigned parity = (unsigned)(n / NST) & 1u;
         // the warp leaves together if any of its lanes' waits ran out (no
         // lane may be left behind at a warp-wide synchronisation)
-        if (!__all_sync(0xffffffffu, wait_bounded(&full[sidx], parity, abort_flag, limit))) {
+        if (!__all_sync(0xffffffffu, wait_bounded(&full[sidx], parity, abort_flag, A.spin_limit))) {
             if (lane == 0 && atomicExch((int*)abort_flag, 1) == 0) atomicOr(A.status, ST_TIMEOUT);
             break;
         }
@@ -374,7 +370,7 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
         if (tid == 0 && producing) {
             // Refill the stage with the tile claimed earlier once every warp
             // has released it; claim the one after that.
-            gave_up = !wait_bounded(&empty[sidx], parity, abort_flag, limit);
+            gave_up = !wait_bounded(&empty[sidx], parity, abort_flag, A.spin_limit);
             if (gave_up) {
                 if (atomicExch((int*)abort_flag, 1) == 0) atomicOr(A.status, ST_TIMEOUT);
                 producing = false;
@@ -390,15 +386,14 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
                 mbar_arrive(&full[sidx]);   // releases the consumers: no tile
                 producing = false;
             }
-#pragma unroll
-            for (int k = 0; k < NST; ++k) fills[k] += k == sidx;
+            ++nfills;
         }
         // warp 0 reconverges after the producer's work, and leaves together
         // with it if its wait ran out
         if (__shfl_sync(0xffffffffu, (int)gave_up, 0)) break;
     }
     // a wait ran out: the copies this CTA issued must land before it exits
-    if (tid == 0 && *abort_flag) drain_fills<NST>(full, fills);
+    if (tid == 0 && *abort_flag) drain_fills<NST>(full, nfills);
 }
 
 // 64 x 16 tiles, 3 stages, 256 threads, 2 CTAs per SM (128 registers).

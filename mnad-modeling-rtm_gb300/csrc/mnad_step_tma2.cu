@@ -245,9 +245,8 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma2(const 
     const int s = A.s;                      // even: this pass runs steps s and s + 1
     const int lc = s & 3, lp = (s + 3) & 3, l1 = (s + 1) & 3, l2 = (s + 2) & 3;
     const int bank = (s >> 1) & 1;
-    const unsigned limit = A.spin_limit ? A.spin_limit : SPIN_LIMIT_DEFAULT;
     int next_claim = -1;
-    unsigned fills[NSTAGE] = {0, 0};
+    unsigned nfills = 0;                    // producer: fills issued; fill f goes to stage f % NSTAGE
     bool gave_up = false;                   // producer: its wait for a free stage ran out
     if (tid == 0) {
         for (int k = 0; k < NSTAGE; ++k) {
@@ -268,7 +267,7 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma2(const 
         for (int k = 0; k < NSTAGE; ++k) {
             if (stage_tile[k] >= 0) issue_tile2(A, stage_tile[k], stages[k], &full[k], lc, lp);
             else mbar_arrive(&full[k]);
-            fills[k] = 1;
+            ++nfills;
         }
     const int tzt = tid % TMA_TZY, txt = tid / TMA_TZY;
 
@@ -277,7 +276,7 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma2(const 
         const unsigned parity = (unsigned)(n >> 1) & 1u;
         // the CTA goes on only if every thread's wait succeeded (the pass has
         // CTA-wide barriers, so nobody may be left behind)
-        const bool ok = gave_up ? false : wait_bounded(&full[sidx], parity, abort_flag, limit);
+        const bool ok = gave_up ? false : wait_bounded(&full[sidx], parity, abort_flag, A.spin_limit);
         if (!__syncthreads_and(ok)) {
             if (tid == 0 && atomicExch((int*)abort_flag, 1) == 0) atomicOr(A.status, ST_TIMEOUT);
             break;
@@ -344,7 +343,7 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma2(const 
         if (lane == 0) mbar_arrive(&empty[sidx]);
         if (tid == 0 && !gave_up) {
             // refill the stage once every warp has released it
-            if (!wait_bounded(&empty[sidx], parity, abort_flag, limit)) {
+            if (!wait_bounded(&empty[sidx], parity, abort_flag, A.spin_limit)) {
                 gave_up = true;     // the next full-barrier check takes the whole CTA out
             } else {
                 const int t2 = next_claim < A.ntiles ? next_claim : -1;
@@ -355,13 +354,12 @@ __global__ void __launch_bounds__(TMA_THREADS, TMA_CTAS_PER_SM) step_tma2(const 
                 } else {
                     mbar_arrive(&full[sidx]);
                 }
-                if (sidx) ++fills[1];
-                else ++fills[0];
+                ++nfills;
             }
         }
     }
     // a wait ran out: the copies this CTA issued must land before it exits
-    if (tid == 0 && *abort_flag) drain_fills<NSTAGE>(full, fills);
+    if (tid == 0 && *abort_flag) drain_fills<NSTAGE>(full, nfills);
 }
 
 size_t step_tma2_smem_bytes() { return OFF_FLAG2 + 16; }

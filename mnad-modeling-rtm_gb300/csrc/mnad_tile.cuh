@@ -85,9 +85,11 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 }
 
 // Bounded wait of at most `limit` polls; gives up early once another thread
-// has aborted.
+// has aborted.  Callers pass the kernel parameter StepArgs::spin_limit itself,
+// which stays a constant-bank operand instead of a register held across the
+// tile loop.
 __device__ __forceinline__ bool wait_bounded(uint64_t* bar, unsigned parity, const volatile int* abort_flag,
-                                             unsigned limit)
+                                             const unsigned& limit)
 {
     for (unsigned it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
@@ -98,16 +100,18 @@ __device__ __forceinline__ bool wait_bounded(uint64_t* bar, unsigned parity, con
 
 // A CTA that gave up waits (bounded) for the last fill it issued on each of
 // its NS stages to land before it exits: a bulk copy must not write into the
-// shared memory of an exited CTA.  fills[k] counts the operations that
-// complete a phase of stage k's full barrier; all but the last had completed
-// before the producer could issue the next.
+// shared memory of an exited CTA.  `nfills` counts the operations that
+// completed or will complete a phase of a full barrier (a tile's copies, or
+// the arrive of "no tile"); fill f went to stage f % NS, and all but the last
+// fill of a stage had completed before the producer could issue the next.
 template <int NS>
-__device__ __forceinline__ void drain_fills(uint64_t* full, const unsigned* fills)
+__device__ __forceinline__ void drain_fills(uint64_t* full, unsigned nfills)
 {
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-        if (fills[k] == 0) continue;
-        const unsigned par = (fills[k] - 1u) & 1u;
+        const unsigned fk = (nfills + (unsigned)(NS - 1 - k)) / NS;     // fills of stage k
+        if (fk == 0) continue;
+        const unsigned par = (fk - 1u) & 1u;
         for (unsigned it = 0; it < DRAIN_LIMIT && !mbar_try_wait(&full[k], par); ++it) __nanosleep(64);
     }
 }
