@@ -11,7 +11,7 @@ illumination = sum of their T*illum, img_RTM = image ./ illumination) are
 compared with the same stacks of the FP64 C/OpenMP oracle.
 
 The oracle part is CPU-bound (16 x 3 propagations of 5.2 M points x 1000
-steps, about 25 minutes on 16 cores), so the three parts run apart:
+steps, about 95 minutes on 8 host cores), so the three parts run apart:
 
   python tests/faulted_salt_subset.py gpu <gpu.npz>        (on a GB300)
   python tests/faulted_salt_subset.py oracle <oracle.npz>  (any host)
