@@ -168,3 +168,43 @@ def test_rtm_shot_against_the_oracle(variant):
     print(f"{variant} kernel vs FP64 oracle: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
     assert errs["gather"] <= TOL_GATHER and errs["gather_bg"] <= TOL_GATHER
     assert errs["illum"] <= TOL_IMAGE and errs["image"] <= TOL_IMAGE
+
+
+def shot_layout(layout):
+    """Receivers of shot() plus, for 'scan', receivers at several depths in
+    columns 20 and 41 (a vertical line: several entries in one bucket column
+    of the adjoint's injection scan), or, for 'duplicates', second receivers
+    at the points (65, 16) and (65, 33) (two injections at one point, added in
+    entry order)."""
+    s = shot(nt=241)
+    extra = {"scan": ([20, 20, 20, 41], [30, 70, 100, 90]), "duplicates": ([16, 33], [65, 65])}[layout]
+    return dict(s, xr=np.concatenate([s["xr"], extra[0]]), zr=np.concatenate([s["zr"], extra[1]]))
+
+
+@pytest.mark.parametrize("layout", ["scan", "duplicates"])
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_adjoint_injection_forms_equal_the_one_step_kernel(layout, variant):
+    s = shot_layout(layout)
+    a = rtm("tma", s, "f32", 3)
+    b = rtm(variant, s, "f32", 3)
+    for x, y, name in zip(a, b, ("gather", "background gather", "UU", "illum", "image")):
+        assert np.linalg.norm(x) > 0, name
+        assert np.array_equal(x, y), f"{name} differs ({layout}): rel {rel(y, x):.2e}"
+
+
+@pytest.mark.parametrize("layout", ["scan", "duplicates"])
+@pytest.mark.parametrize("kernel", ["tma", "direct"])
+def test_adjoint_injection_forms_against_the_oracle(layout, kernel):
+    s = shot_layout(layout)
+    T = 3
+    nf = P.snapshot_nf(s["vs"], s["nt"])
+    ncols = max(2 * nf + 1, s["nt"] // T)
+    a = (s["dx"], s["xs"], s["xr"], s["dz"], s["zs"], s["zr"])
+    data = coracle.fwd(*a, s["v"], s["dt"], s["nt"], s["w"], s["d"])["datau"]
+    bg = coracle.fwd(*a, s["vs"], s["dt"], s["nt"], s["w"], s["d"], indx=1, T=T, ncols=ncols)
+    im = coracle.adj(s["dx"], s["dz"], s["nt"], s["dt"], s["vs"], s["xr"], s["zr"], data - bg["datau"], s["d"],
+                     bg["UU"], T)
+    img = rtm(kernel, s, "f32", T)[4]
+    err = rel(img, im)
+    print(f"{layout} receivers, {kernel} kernel: image rel-L2 {err:.2e}")
+    assert err <= TOL_IMAGE
