@@ -121,7 +121,8 @@ MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const d
 {
     return guard([&] {
         need(ctx != nullptr, "context is NULL");
-        check_grid(nz, nx, d_pml, nt, dx, dz, dt, v);
+        ModelScans scans;                   // the model is scanned once: checks, then its min / max
+        check_grid(nz, nx, d_pml, nt, dx, dz, dt, v, &scans);
         need(w != nullptr, "w is NULL");
         need(nr == 0 || datau != nullptr, "datau is NULL");
         need(indx == 0 || indx == 1, "indx must be 0 or 1");
@@ -138,8 +139,7 @@ MNAD_API int mnad_fwd_pde_exact(mnad_context* ctx, double dx, double xs, const d
         s.energy_every = c.opt.energy_every;
         std::unique_ptr<Wavefield> wf;
         if (indx == 1) {
-            double vmin, vmax;
-            model_minmax(v, (size_t)nz * nx, vmin, vmax);
+            const auto [vmin, vmax] = scans.scan(v, (size_t)nz * nx);
             const int nf = snapshot_nf(nt, vmin, vmax);                     // :46
             const int T = c.opt.T > 0 ? c.opt.T : snapshot_T(nt, nf);       // :47
             const int k = nt / T;
@@ -254,7 +254,8 @@ MNAD_API int mnad_born_adj(mnad_context* ctx, double dx, double dz, int nt, doub
 {
     return guard([&] {
         need(ctx != nullptr, "context is NULL");
-        check_grid(nz, nx, d_pml, nt, dx, dz, dt, v);
+        ModelScans scans;                   // the model is scanned once: checks, then its min / max
+        check_grid(nz, nx, d_pml, nt, dx, dz, dt, v, &scans);
         need(im != nullptr, "im is NULL");
         need(nr == 0 || data != nullptr, "data is NULL");
         Context& c = *ctx;
@@ -266,8 +267,7 @@ MNAD_API int mnad_born_adj(mnad_context* ctx, double dx, double dz, int nt, doub
         Wavefield& wf = *it->second;
         need(wf.nint == (size_t)(nz - 2 * d_pml) * (nx - 2 * d_pml),
              "stored wavefield of shot " + std::to_string(ss) + " has a different interior size");
-        double vmin, vmax;
-        model_minmax(v, (size_t)nz * nx, vmin, vmax);
+        const auto [vmin, vmax] = scans.scan(v, (size_t)nz * nx);
         const int T = c.opt.T > 0 ? c.opt.T : snapshot_T(nt, snapshot_nf(nt, vmin, vmax));   // :41-42
         need(nt / T <= wf.ncols, "more imaging steps (floor(nt/T)) than snapshot columns; "
                                  "UU(:,end-ttt+1) would index column < 1");
@@ -541,7 +541,8 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
         auto P = std::make_unique<mnad_plan>();
         P->ctx = ctx;
         P->jobs.assign(jobs, jobs + njobs);
-        for (int k = 0; k < njobs; ++k) check_job(jobs[k], k);
+        ModelScans scans;                   // each distinct model is scanned once
+        for (int k = 0; k < njobs; ++k) check_job(jobs[k], k, &scans);
         const TileCfg tc = tile_cfg(c.opt.kernel);
         P->ckpt = c.opt.checkpoint_every > 0;
         // whole runs from step 0: the phases may use the two-step kernel
@@ -562,7 +563,7 @@ MNAD_API int mnad_plan_create(mnad_context* ctx, const mnad_job* jobs, int njobs
             P->fwd_true[k] = add_prop(*P, j, MODE_FWD, j.v, nullptr, 0);
             if (j.kind == MNAD_JOB_RTM) {
                 int T, ncols;
-                rtm_snapshot_plan(j, T, ncols);
+                rtm_snapshot_plan(j, T, ncols, &scans);
                 const int k_snap = j.nt / T;
                 if (P->ckpt) {
                     // segments of C = m*T steps (C even, so a restored state keeps

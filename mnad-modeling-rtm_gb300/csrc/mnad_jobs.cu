@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <tuple>
 #include <vector>
 
 #include "mnad_kernels.h"
@@ -29,7 +30,22 @@ int index1(double x, int n, const char* what)
     return (int)x - 1;
 }
 
-void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, const double* v)
+std::pair<double, double> ModelScans::scan(const double* v, size_t n)
+{
+    const auto key = std::make_pair(v, n);
+    const auto it = seen.find(key);
+    if (it != seen.end()) return it->second;
+    double vmin = INFINITY, vmax = -INFINITY;
+    for (size_t k = 0; k < n; ++k) {
+        if (!(std::isfinite(v[k]) && v[k] > 0))   // the message is built only on failure
+            need(false, "velocity must be positive and finite (entry " + std::to_string(k) + ")");
+        vmin = std::min(vmin, v[k]);
+        vmax = std::max(vmax, v[k]);
+    }
+    return seen.emplace(key, std::make_pair(vmin, vmax)).first->second;
+}
+
+void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, const double* v, ModelScans* scans)
 {
     need(v != nullptr, "v is NULL");
     need(nz >= 1 && nx >= 1, "grid must be at least 1 x 1");
@@ -38,6 +54,10 @@ void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, 
     need(std::isfinite(dx) && dx > 0 && std::isfinite(dz) && dz > 0 && std::isfinite(dt) && dt > 0,
          "dx, dz, dt must be positive and finite");
     const size_t n = (size_t)nz * nx;
+    if (scans) {
+        scans->scan(v, n);
+        return;
+    }
     for (size_t k = 0; k < n; ++k)
         if (!(std::isfinite(v[k]) && v[k] > 0))   // the message is built only on failure
             need(false, "velocity must be positive and finite (entry " + std::to_string(k) + ")");
@@ -78,14 +98,14 @@ void fill_receivers(PropSpec& s, const double* xr, const double* zr, int nr)
     }
 }
 
-void check_job(const mnad_job& j, int k)
+void check_job(const mnad_job& j, int k, ModelScans* scans)
 {
     const std::string pre = "job " + std::to_string(k) + ": ";
     need(j.kind == MNAD_JOB_MODEL || j.kind == MNAD_JOB_RTM, pre + "kind must be MNAD_JOB_MODEL or MNAD_JOB_RTM");
-    check_grid(j.nz, j.nx, j.d_pml, j.nt, j.dx, j.dz, j.dt, j.v);
+    check_grid(j.nz, j.nx, j.d_pml, j.nt, j.dx, j.dz, j.dt, j.v, scans);
     need(j.w != nullptr, pre + "w is NULL");
     if (j.kind == MNAD_JOB_RTM) {
-        check_grid(j.nz, j.nx, j.d_pml, j.nt, j.dx, j.dz, j.dt, j.vs);
+        check_grid(j.nz, j.nx, j.d_pml, j.nt, j.dx, j.dz, j.dt, j.vs, scans);
         need(j.image_out != nullptr, pre + "image_out is NULL");
     } else {
         need(j.nr == 0 || j.data_out != nullptr, pre + "data_out is NULL");
@@ -93,10 +113,11 @@ void check_job(const mnad_job& j, int k)
 }
 
 
-void rtm_snapshot_plan(const mnad_job& j, int& T, int& ncols)
+void rtm_snapshot_plan(const mnad_job& j, int& T, int& ncols, ModelScans* scans)
 {
     double vmin, vmax;
-    model_minmax(j.vs, (size_t)j.nz * j.nx, vmin, vmax);
+    if (scans) std::tie(vmin, vmax) = scans->scan(j.vs, (size_t)j.nz * j.nx);
+    else model_minmax(j.vs, (size_t)j.nz * j.nx, vmin, vmax);
     const int nf = snapshot_nf(j.nt, vmin, vmax);             // fwd_PDE_exact_MNAD.m:46
     T = j.T > 0 ? j.T : snapshot_T(j.nt, nf);                  // :47
     ncols = std::max(2 * nf + 1, j.nt / T);                    // :53 (grown to k when larger)

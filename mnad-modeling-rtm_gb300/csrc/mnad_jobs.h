@@ -1,9 +1,11 @@
 // Argument checking, error capture and job set-up shared by the C ABI entry
 // points (mnad_capi.cu) and the serving loop (mnad_server.cu).  Internal.
 #pragma once
+#include <map>
 #include <memory>
 #include <new>
 #include <string>
+#include <utility>
 
 #include "mnad_engine.h"
 
@@ -34,15 +36,23 @@ int guard(F&& f)
 void need(bool ok, const std::string& msg);
 // 1-based grid index passed as a double (MATLAB) -> 0-based int.
 int index1(double x, int n, const char* what);
-void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, const double* v);
-void check_job(const mnad_job& j, int k);
+// Velocity models scanned during one call.  The jobs of a batch usually
+// share their models, so each distinct array is checked (positive, finite)
+// and its min / max taken once per call instead of once per job.
+struct ModelScans {
+    std::map<std::pair<const double*, size_t>, std::pair<double, double>> seen;   // -> (vmin, vmax)
+    std::pair<double, double> scan(const double* v, size_t n);
+};
+void check_grid(int nz, int nx, int d, int nt, double dx, double dz, double dt, const double* v,
+                ModelScans* scans = nullptr);
+void check_job(const mnad_job& j, int k, ModelScans* scans = nullptr);
 void fill_receivers(PropSpec& s, const double* xr, const double* zr, int nr);
 // `held` snapshot columns are allocated (< 0: all nsnap).
 std::unique_ptr<Wavefield> new_wavefield(Context& c, int nz, int nx, int d, int nt, int T, int ncols, int nsnap,
                                          int codec, int held = -1);
 // Snapshot interval of an RTM job (job.T or the reference formula on vs)
 // and the UU column count max(2 nf + 1, floor(nt/T)).
-void rtm_snapshot_plan(const mnad_job& j, int& T, int& ncols);
+void rtm_snapshot_plan(const mnad_job& j, int& T, int& ncols, ModelScans* scans = nullptr);
 // Propagation spec of a job: forward (true or background model) or adjoint.
 PropSpec job_spec(const mnad_job& j, int mode, const double* v, Wavefield* wf, int T, int pairing);
 // Device status bits -> error: ST_TIMEOUT throws MNAD_E_TIMEOUT (a step
