@@ -25,8 +25,9 @@ void need(bool ok, const std::string& msg)
 // 1-based grid index passed as a double (MATLAB) -> 0-based int.
 int index1(double x, int n, const char* what)
 {
-    need(std::isfinite(x) && x == std::floor(x) && x >= 1 && x <= n,
-         std::string(what) + " must be an integer grid index in [1, " + std::to_string(n) + "], got " + std::to_string(x));
+    if (!(std::isfinite(x) && x == std::floor(x) && x >= 1 && x <= n))   // the message is built only on failure
+        need(false, std::string(what) + " must be an integer grid index in [1, " + std::to_string(n) + "], got " +
+                        std::to_string(x));
     return (int)x - 1;
 }
 
