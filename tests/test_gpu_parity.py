@@ -197,6 +197,29 @@ def test_plan_rerun_is_deterministic(ctx):
     plan.close()
 
 
+def test_plan_checks_every_model_once_and_names_the_bad_one(ctx):
+    """Jobs of a plan that share one model array are checked once; a job with
+    its own model holding a NaN still fails the plan with E_ARG."""
+    g = np.load(os.path.join(GOLDEN, "golden_rtm_small.npz"))
+    common = dict(dx=float(g["dx"]), dz=float(g["dz"]), dt=float(g["dt"]), nt=int(g["nt"]), d_pml=int(g["d"]),
+                  zs=int(g["zs"]), xs=int(g["xs"]), zr=g["zr"], xr=g["xr"], w=g["w"])
+    v, vs = np.asfortranarray(g["v"]), np.asfortranarray(g["vs"])
+    bad = vs.copy(order="F")
+    bad[5, 7] = np.nan
+    jobs = [mnad.ShotJob(kind="rtm", v=v, vs=vs, **common), mnad.ShotJob(kind="rtm", v=v, vs=vs, **common),
+            mnad.ShotJob(kind="rtm", v=v, vs=bad, **common)]
+    with pytest.raises(mnad.MnadError) as e:
+        ctx.plan(jobs)
+    assert e.value.code == _lib.E_ARG
+    assert f"velocity must be positive and finite (entry {5 + 7 * v.shape[0]})" in str(e.value)
+    plan = ctx.plan(jobs[:2])             # the two shots of one model run alike
+    plan.run()
+    plan.download()
+    assert np.array_equal(jobs[0].image, jobs[1].image)
+    assert rel(jobs[0].image, g["Im"]) <= TOL_IMAGE
+    plan.close()
+
+
 def test_wavefield_export_import_round_trip(ctx):
     g = np.load(os.path.join(GOLDEN, "golden_rtm_small.npz"))
     nz, nx = g["vs"].shape
@@ -218,14 +241,19 @@ def test_errors_are_reported_not_crashed(ctx):
     with pytest.raises(mnad.MnadError) as e:
         ctx.fwd(10.0, nx + 1, [1], 10.0, 1, [1], v, 1e-3, 10, np.zeros(10), 4)
     assert e.value.code == _lib.E_ARG
+    assert f"xs must be an integer grid index in [1, {nx}]" in str(e.value)
     with pytest.raises(mnad.MnadError) as e:
         ctx.fwd(10.0, 2.5, [1], 10.0, 1, [1], v, 1e-3, 10, np.zeros(10), 4)
     assert e.value.code == _lib.E_ARG
+    with pytest.raises(mnad.MnadError) as e:
+        ctx.fwd(10.0, 5, [1, nx + 3], 10.0, 5, [1, 1], v, 1e-3, 10, np.zeros(10), 4)
+    assert e.value.code == _lib.E_ARG and "xr must be an integer grid index" in str(e.value)
     bad = v.copy()
     bad[3, 3] = np.nan
     with pytest.raises(mnad.MnadError) as e:
         ctx.fwd(10.0, 5, [1], 10.0, 5, [1], bad, 1e-3, 10, np.zeros(10), 4)
     assert e.value.code == _lib.E_ARG
+    assert f"velocity must be positive and finite (entry {3 + 3 * nz})" in str(e.value)
     with pytest.raises(mnad.MnadError) as e:
         ctx.adj(10.0, 10.0, 10, 1e-3, v, [1], [1], np.zeros((10, 1)), 4, ss=12345)
     assert e.value.code == _lib.E_NOTFOUND
