@@ -180,6 +180,22 @@ static CUtensorMap field_map(const float* base, int ld, int ncols, int bz, int b
     return m;
 }
 
+// 3-D map over the three fields of one time level (U at base, V and W at
+// base + fs and base + 2 fs floats): boxes of bz x bx x 3.
+static CUtensorMap fields_map(const float* base, int ld, int ncols, size_t fs, int bz, int bx)
+{
+    CUtensorMap m;
+    cuuint64_t dims[3] = {(cuuint64_t)ld, (cuuint64_t)ncols, 3};
+    cuuint64_t strides[2] = {(cuuint64_t)ld * sizeof(float), (cuuint64_t)fs * sizeof(float)};
+    cuuint32_t box[3] = {(cuuint32_t)bz, (cuuint32_t)bx, 3};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides,
+                                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(MNAD_E_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return m;
+}
+
 void model_minmax(const double* v, size_t n, double& vmin, double& vmax)
 {
     vmin = INFINITY; vmax = -INFINITY;
@@ -623,10 +639,14 @@ void Batch::finalize()
                         maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA2_BOX_Z, TMA2_BOX_X_RING));
                 maps.push_back(field_map(D.r, D.ld, ncols, TMA2_BOX_Z, TMA2_BOX_X_RING));
             } else {
-                for (int t = 0; t < 2; ++t)
-                    for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ + 8, tx_w + 4));
-                for (int t = 0; t < 2; ++t)
-                    for (int f = 0; f < 3; ++f) maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA_TZ, tx_w));
+                // the three fields of a level are one array of stride fs
+                const size_t fs = (size_t)(D.fld[0][1] - D.fld[0][0]);
+                for (int t = 0; t < 2; ++t) {
+                    if (D.fld[t][1] - D.fld[t][0] != (ptrdiff_t)fs || D.fld[t][2] - D.fld[t][1] != (ptrdiff_t)fs)
+                        throw Error(MNAD_E_CUDA, "the fields of a time level are not evenly spaced");
+                    maps.push_back(fields_map(D.fld[t][0], D.ld, ncols, fs, TMA_TZ + 8, tx_w + 4));
+                }
+                for (int t = 0; t < 2; ++t) maps.push_back(fields_map(D.fld[t][0], D.ld, ncols, fs, TMA_TZ, tx_w));
                 maps.push_back(field_map(D.r, D.ld, ncols, TMA_TZ, tx_w));
             }
             // The region whose points a tile computes: the tile itself (one

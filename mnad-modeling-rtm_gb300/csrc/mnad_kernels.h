@@ -24,9 +24,10 @@ constexpr int TMA_CTAS_PER_SM = 2;
 // receiver-bucket tile), 128 threads and 2 stages per CTA, 4 CTAs per SM.
 constexpr int TMA_TX_NARROW = 8, TMA_STAGES_NARROW = 2, TMA_CTAS_PER_SM_NARROW = 4;
 static_assert(TMA_TX % TMA_TX_NARROW == 0, "narrow tiles nest in receiver-bucket tiles");
-// Tensor maps of one propagation: halo boxes of U,V,W at both time levels,
-// point boxes of U,V,W at both levels, point box of r.
-constexpr int TMAP_HALO = 0, TMAP_POINT = 6, TMAP_R = 12, TMAPS_PER_PROP = 13;
+// Tensor maps of one propagation: per time level one 3-D map over U, V, W
+// (the three fields of a level lie at one stride) with the halo box, the same
+// with the point box, and the point box of r -- three copies per tile.
+constexpr int TMAP_HALO = 0, TMAP_POINT = 2, TMAP_R = 4, TMAPS_PER_PROP = 5;
 // Tensor maps of one propagation for the two-step kernel: U, V, W of the four
 // time levels as 72 x 24 boxes (tile + 4-point halo), the same as 72 x 20 boxes
 // (tile + 2-point ring), r as a 72 x 20 box.

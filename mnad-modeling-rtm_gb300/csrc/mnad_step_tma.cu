@@ -73,11 +73,9 @@ __device__ __forceinline__ void issue_tile(const StepArgs& A, int t, Stage<TX>& 
     mbar_expect_tx(bar, Stage<TX>::BYTES);
     bulk_load(&st.desc, A.props + pi, sizeof(PropDesc), bar);
     bulk_load(&st.info, A.tile_info + t, sizeof(int4), bar);
-#pragma unroll
-    for (int f = 0; f < 3; ++f) tma_load_2d(&st.halo[f][0][0], maps + TMAP_HALO + cur * 3 + f, bar, j0, i0);
-#pragma unroll
-    for (int f = 0; f < 3; ++f)
-        tma_load_2d(&st.pts[f][0][0], maps + TMAP_POINT + (cur ^ 1) * 3 + f, bar, j0 + HZ, i0 + HX);
+    // U, V, W of a level in one 3-D box each: [f][x][z] is the stage's layout
+    tma_load_3d(&st.halo[0][0][0], maps + TMAP_HALO + cur, bar, j0, i0, 0);
+    tma_load_3d(&st.pts[0][0][0], maps + TMAP_POINT + (cur ^ 1), bar, j0 + HZ, i0 + HX, 0);
     tma_load_2d(&st.pts[3][0][0], maps + TMAP_R, bar, j0 + HZ, i0 + HX);
 }
 
