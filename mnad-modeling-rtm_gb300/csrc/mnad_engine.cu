@@ -630,22 +630,21 @@ void Batch::finalize()
             all.push_back(D);
             if (!tma) continue;
             const int ncols = D.nx + 2 * HX;
+            // the three fields of a level are one array of stride fs
+            const int levels = tma2 ? 4 : 2;
+            const size_t fs = (size_t)(D.fld[0][1] - D.fld[0][0]);
+            for (int t = 0; t < levels; ++t)
+                if (D.fld[t][1] - D.fld[t][0] != (ptrdiff_t)fs || D.fld[t][2] - D.fld[t][1] != (ptrdiff_t)fs)
+                    throw Error(MNAD_E_CUDA, "the fields of a time level are not evenly spaced");
             if (tma2) {
                 for (int t = 0; t < 4; ++t)
-                    for (int f = 0; f < 3; ++f)
-                        maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA2_BOX_Z, TMA2_BOX_X_CUR));
+                    maps.push_back(fields_map(D.fld[t][0], D.ld, ncols, fs, TMA2_BOX_Z, TMA2_BOX_X_CUR));
                 for (int t = 0; t < 4; ++t)
-                    for (int f = 0; f < 3; ++f)
-                        maps.push_back(field_map(D.fld[t][f], D.ld, ncols, TMA2_BOX_Z, TMA2_BOX_X_RING));
+                    maps.push_back(fields_map(D.fld[t][0], D.ld, ncols, fs, TMA2_BOX_Z, TMA2_BOX_X_RING));
                 maps.push_back(field_map(D.r, D.ld, ncols, TMA2_BOX_Z, TMA2_BOX_X_RING));
             } else {
-                // the three fields of a level are one array of stride fs
-                const size_t fs = (size_t)(D.fld[0][1] - D.fld[0][0]);
-                for (int t = 0; t < 2; ++t) {
-                    if (D.fld[t][1] - D.fld[t][0] != (ptrdiff_t)fs || D.fld[t][2] - D.fld[t][1] != (ptrdiff_t)fs)
-                        throw Error(MNAD_E_CUDA, "the fields of a time level are not evenly spaced");
+                for (int t = 0; t < 2; ++t)
                     maps.push_back(fields_map(D.fld[t][0], D.ld, ncols, fs, TMA_TZ + 8, tx_w + 4));
-                }
                 for (int t = 0; t < 2; ++t) maps.push_back(fields_map(D.fld[t][0], D.ld, ncols, fs, TMA_TZ, tx_w));
                 maps.push_back(field_map(D.r, D.ld, ncols, TMA_TZ, tx_w));
             }

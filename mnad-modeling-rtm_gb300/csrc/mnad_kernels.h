@@ -28,10 +28,10 @@ static_assert(TMA_TX % TMA_TX_NARROW == 0, "narrow tiles nest in receiver-bucket
 // (the three fields of a level lie at one stride) with the halo box, the same
 // with the point box, and the point box of r -- three copies per tile.
 constexpr int TMAP_HALO = 0, TMAP_POINT = 2, TMAP_R = 4, TMAPS_PER_PROP = 5;
-// Tensor maps of one propagation for the two-step kernel: U, V, W of the four
-// time levels as 72 x 24 boxes (tile + 4-point halo), the same as 72 x 20 boxes
-// (tile + 2-point ring), r as a 72 x 20 box.
-constexpr int TMAP2_CUR = 0, TMAP2_RING = 12, TMAP2_R = 24, TMAPS_PER_PROP2 = 25;
+// Tensor maps of one propagation for the two-step kernel: per time level (four)
+// one 3-D map over U, V, W with 72 x 24 boxes (tile + 4-point halo), the same
+// with 72 x 20 boxes (tile + 2-point ring), r as a 72 x 20 box.
+constexpr int TMAP2_CUR = 0, TMAP2_RING = 4, TMAP2_R = 8, TMAPS_PER_PROP2 = 9;
 constexpr int TMA2_BOX_Z = TMA_TZ + 8, TMA2_BOX_X_CUR = TMA_TX + 8, TMA2_BOX_X_RING = TMA_TX + 4;
 // tile_info.z flags
 constexpr int TILE_STRIP = 1;         // intersects a CPML strip or the grid edge

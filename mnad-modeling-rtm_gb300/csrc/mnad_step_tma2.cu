@@ -83,10 +83,8 @@ __device__ __forceinline__ void issue_tile2(const StepArgs& A, int t, Stage2& st
     mbar_expect_tx(bar, STAGE_BYTES2);
     bulk_load(&st.desc, A.props + pi, sizeof(PropDesc), bar);
     bulk_load(&st.info, A.tile_info + t, sizeof(int4), bar);
-#pragma unroll
-    for (int f = 0; f < 3; ++f) tma_load_2d(&st.cur[f][0][0], maps + TMAP2_CUR + lc * 3 + f, bar, j0, i0 + HX - 4);
-#pragma unroll
-    for (int f = 0; f < 3; ++f) tma_load_2d(&st.ring[f][0][0], maps + TMAP2_RING + lp * 3 + f, bar, j0, i0 + HX - 2);
+    tma_load_3d(&st.cur[0][0][0], maps + TMAP2_CUR + lc, bar, j0, i0 + HX - 4, 0);
+    tma_load_3d(&st.ring[0][0][0], maps + TMAP2_RING + lp, bar, j0, i0 + HX - 2, 0);
     tma_load_2d(&st.r[0][0], maps + TMAP2_R, bar, j0, i0 + HX - 2);
 }
 
