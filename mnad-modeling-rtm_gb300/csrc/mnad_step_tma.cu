@@ -116,6 +116,10 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
     // producer: operations issued that complete a phase of a full barrier (a
     // tile's copies, or the arrive of "no tile"); fill f goes to stage f % NST
     unsigned nfills = 0;
+    // The first NST tiles of CTA b are b, b + grid, ... (no claim to wait
+    // for before the first copies); later tiles are claimed from the counter,
+    // which numbers the tiles after those.
+    const int first = NST * (int)gridDim.x;
     if (tid == 0) {
         for (int k = 0; k < NST; ++k) {
             mbar_init(&full[k], 1);
@@ -123,20 +127,17 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
         }
         fence_mbar_init();
         *abort_flag = 0;
-        for (int k = 0; k < NST; ++k) {
-            const int t = atomicAdd(A.tile_counter, 1);
-            stage_tile[k] = t < A.ntiles ? t : -1;
-        }
-        next_claim = atomicAdd(A.tile_counter, 1);
-    }
-    __syncthreads();
-    if (tid == 0)
 #pragma unroll
         for (int k = 0; k < NST; ++k) {
-            if (stage_tile[k] >= 0) issue_tile<TX>(A, stage_tile[k], stages[k], &full[k], cur);
+            const int t = (int)blockIdx.x + k * (int)gridDim.x;
+            stage_tile[k] = t < A.ntiles ? t : -1;
+            if (t < A.ntiles) issue_tile<TX>(A, t, stages[k], &full[k], cur);
             else mbar_arrive(&full[k]);     // releases the consumers: no tile
             ++nfills;
         }
+        next_claim = first + atomicAdd(A.tile_counter, 1);
+    }
+    __syncthreads();
     const int tzt = tid % TMA_TZY, txt = tid / TMA_TZY;
     const int c = txt + 2, r0 = tzt * TMA_PZ + 4;
     bool producing = true;
@@ -379,7 +380,7 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
             stage_tile[sidx] = t2;
             if (t2 >= 0) {
                 issue_tile<TX>(A, t2, stages[sidx], &full[sidx], cur);
-                next_claim = atomicAdd(A.tile_counter, 1);
+                next_claim = first + atomicAdd(A.tile_counter, 1);
             } else {
                 mbar_arrive(&full[sidx]);   // releases the consumers: no tile
                 producing = false;
