@@ -157,6 +157,7 @@ struct StepArgs {
     int ntiles;
     int ntz;               // tiles along z of every propagation of the group
     int tiles_per_prop;    // ntz * ntx (one geometry per launch group)
+    float inv_tiles_per_prop, inv_ntz;   // 1/tiles_per_prop, 1/ntz: division-free tile decode
     int s;                 // global step index
     unsigned* status;      // launch-wide status word (ST_TIMEOUT: the launch did not finish its tiles)
     unsigned spin_limit;   // polls of a bounded barrier wait before it gives up (persistent kernels; set by the host, > 0)

@@ -681,6 +681,8 @@ void Batch::finalize()
                                              j0 | (i0 << 16)));
                 }
         }
+        if (tile_prop.size() >= (size_t(1) << 24))   // the kernels decode tile numbers through float
+            throw Error(MNAD_E_ARG, "a launch group holds 2^24 tiles or more; split the batch");
         g->ntiles = (int)tile_prop.size();
         ntiles_ += g->ntiles;
         g->desc = DevMem(&ctx_, descs.size() * sizeof(PropDesc));
@@ -838,6 +840,8 @@ void Batch::launch_group(size_t gi, int s, int slot)
         a.ntiles = g->ntiles;
         a.ntz = g->ntz;
         a.tiles_per_prop = g->tiles_per_prop;
+        a.inv_tiles_per_prop = 1.0f / (float)std::max(1, g->tiles_per_prop);
+        a.inv_ntz = 1.0f / (float)std::max(1, g->ntz);
         a.s = s;
         a.status = ctx_.d_status;
         a.spin_limit = ctx_.wait_limit ? ctx_.wait_limit : SPIN_LIMIT_DEFAULT;

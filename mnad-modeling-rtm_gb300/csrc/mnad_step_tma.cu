@@ -66,9 +66,10 @@ static_assert(sizeof(PropDesc) % 16 == 0, "bulk copies move multiples of 16 byte
 template <int TX>
 __device__ __forceinline__ void issue_tile(const StepArgs& A, int t, Stage<TX>& st, uint64_t* bar, int cur)
 {
-    const int pi = t / A.tiles_per_prop;
+    const int pi = div_small(t, A.tiles_per_prop, A.inv_tiles_per_prop);
     const int tl = t - pi * A.tiles_per_prop;
-    const int j0 = (tl % A.ntz) * TMA_TZ, i0 = (tl / A.ntz) * TX;
+    const int tx = div_small(tl, A.ntz, A.inv_ntz);
+    const int j0 = (tl - tx * A.ntz) * TMA_TZ, i0 = tx * TX;
     const CUtensorMap* maps = static_cast<const CUtensorMap*>(A.tmaps) + (size_t)pi * TMAPS_PER_PROP;
     mbar_expect_tx(bar, Stage<TX>::BYTES);
     bulk_load(&st.desc, A.props + pi, sizeof(PropDesc), bar);

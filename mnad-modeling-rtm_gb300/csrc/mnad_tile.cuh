@@ -125,6 +125,19 @@ __device__ __forceinline__ void drain_fills(uint64_t* full, unsigned nfills)
     }
 }
 
+// n / d for 0 <= n < 2^24, d >= 1, from a float reciprocal of d: float(n) is
+// exact and the estimate is within 2 of the quotient, which two corrections
+// each way make exact (no integer division on the producer's path).
+__device__ __forceinline__ int div_small(int n, int d, float inv_d)
+{
+    int q = (int)((float)n * inv_d);
+    q -= q * d > n;
+    q -= q * d > n;
+    q += (q + 1) * d <= n;
+    q += (q + 1) * d <= n;
+    return q;
+}
+
 // ---- register window and packed stencil arithmetic ------------------------
 // TMA_PZ consecutive floats (16-byte aligned) to / from registers.
 __device__ __forceinline__ void ldv(const float* p, float* o)
