@@ -80,15 +80,18 @@ __device__ __forceinline__ void issue_tile(const StepArgs& A, int t, Stage<TX>& 
     tma_load_2d(&st.pts[3][0][0], maps + TMAP_R, bar, j0 + HZ, i0 + HX);
 }
 
-// Shared-memory layout: NST stages, their full and empty barriers, the tile
-// held by each stage, the abort flag.
+// Shared-memory layout: NST stages and their full barriers; per stage the
+// count of warps that released it, the tile claimed for its next fill and
+// the tile it holds; the abort flag; the count of fills issued.
 template <int TX, int NST>
 struct Layout {
     static constexpr size_t FULL = NST * sizeof(Stage<TX>);
-    static constexpr size_t EMPTY = FULL + NST * sizeof(uint64_t);
-    static constexpr size_t TILE = EMPTY + NST * sizeof(uint64_t);
+    static constexpr size_t REL = FULL + NST * sizeof(uint64_t);
+    static constexpr size_t NEXT = REL + NST * sizeof(int);
+    static constexpr size_t TILE = NEXT + NST * sizeof(int);
     static constexpr size_t FLAG = TILE + NST * sizeof(int);
-    static constexpr size_t BYTES = FLAG + 16;
+    static constexpr size_t NFILL = FLAG + sizeof(int);
+    static constexpr size_t BYTES = NFILL + 16;
 };
 
 }  // namespace
@@ -104,19 +107,23 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     St* stages = reinterpret_cast<St*>(smem_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + L::FULL);
-    uint64_t* empty = reinterpret_cast<uint64_t*>(smem_raw + L::EMPTY);
+    int* released = reinterpret_cast<int*>(smem_raw + L::REL);
+    volatile int* next_tile = reinterpret_cast<volatile int*>(smem_raw + L::NEXT);
     volatile int* stage_tile = reinterpret_cast<volatile int*>(smem_raw + L::TILE);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + L::FLAG);
+    unsigned* nfills = reinterpret_cast<unsigned*>(smem_raw + L::NFILL);
     const int tid = threadIdx.x, lane = tid & 31;
     if (smem_addr(smem_raw) & 127u) {       // TMA destinations need aligned stages
         if (tid == 0 && A.ntiles > 0) atomicOr(A.status, ST_TIMEOUT);
         return;
     }
     const int cur = A.s & 1;
-    int next_claim = -1;                    // producer: tile claimed one refill ahead
-    // producer: operations issued that complete a phase of a full barrier (a
-    // tile's copies, or the arrive of "no tile"); fill f goes to stage f % NST
-    unsigned nfills = 0;
+    // Thread 0 claims tiles from the launch's counter, one per iteration and
+    // one iteration ahead (the atomic's latency stays off its path); the claim
+    // goes to next_tile[stage] for the stage's next fill.  The last warp to
+    // release a stage refills it, so the producer work of a tile falls on
+    // whichever warp finished it last rather than always on warp 0.
+    int next_claim = -1;
     // The first NST tiles of CTA b are b, b + grid, ... (no claim to wait
     // for before the first copies); later tiles are claimed from the counter,
     // which numbers the tiles after those.
@@ -124,7 +131,7 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
     if (tid == 0) {
         for (int k = 0; k < NST; ++k) {
             mbar_init(&full[k], 1);
-            mbar_init(&empty[k], NWARPS);
+            released[k] = 0;
         }
         fence_mbar_init();
         *abort_flag = 0;
@@ -134,14 +141,15 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
             stage_tile[k] = t < A.ntiles ? t : -1;
             if (t < A.ntiles) issue_tile<TX>(A, t, stages[k], &full[k], cur);
             else mbar_arrive(&full[k]);     // releases the consumers: no tile
-            ++nfills;
         }
+        // operations that complete a phase of a full barrier (a tile's
+        // copies, or the arrive of "no tile"); fill f goes to stage f % NST
+        *nfills = NST;
         next_claim = first + atomicAdd(A.tile_counter, 1);
     }
     __syncthreads();
     const int tzt = tid % TMA_TZY, txt = tid / TMA_TZY;
     const int c = txt + 2, r0 = tzt * TMA_PZ + 4;
-    bool producing = true;
 
     for (int n = 0;; ++n) {
         const int sidx = n % NST;
@@ -152,8 +160,12 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
             if (lane == 0 && atomicExch((int*)abort_flag, 1) == 0) atomicOr(A.status, ST_TIMEOUT);
             break;
         }
-        const int t = stage_tile[sidx];      // written before the producer's arrive
+        const int t = stage_tile[sidx];      // written before the refill's arrive
         if (t < 0) break;
+        if (tid == 0) {                      // the claim for this stage's next fill
+            next_tile[sidx] = next_claim;
+            next_claim = first + atomicAdd(A.tile_counter, 1);
+        }
         const St& st = stages[sidx];
         const PropDesc& P = st.desc;
         const int4 info = st.info;
@@ -363,37 +375,37 @@ __device__ __forceinline__ void step_tma_body(const StepArgs& A)
             stv(P.fld[cur ^ 1][1] + p, ov);
             stv(P.fld[cur ^ 1][2] + p, ow);
         }
-        // This warp is done with the stage.
+        // This warp is done with the stage: its reads are ordered before the
+        // release (warp barrier, then a CTA-scope fence before the count).
         __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[sidx]);
-        bool gave_up = false;
-        if (tid == 0 && producing) {
-            // Refill the stage with the tile claimed earlier once every warp
-            // has released it; claim the one after that.
-            gave_up = !wait_bounded(&empty[sidx], parity, abort_flag, A.spin_limit);
-            if (gave_up) {
-                if (atomicExch((int*)abort_flag, 1) == 0) atomicOr(A.status, ST_TIMEOUT);
-                producing = false;
-            }
+        int last = 0;
+        if (lane == 0) {
+            __threadfence_block();
+            last = atomicAdd(&released[sidx], 1) == NWARPS - 1;
         }
-        if (tid == 0 && producing) {
-            const int t2 = next_claim < A.ntiles ? next_claim : -1;
-            stage_tile[sidx] = t2;
-            if (t2 >= 0) {
+        if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
+            // Every warp has released the stage: refill it with the tile
+            // thread 0 claimed for it in this iteration.
+            released[sidx] = 0;
+            __threadfence_block();
+            fence_proxy_async_smem();       // the reads above come before the copies' writes
+            const int t2 = next_tile[sidx];
+            if (t2 < A.ntiles) {
+                stage_tile[sidx] = t2;
                 issue_tile<TX>(A, t2, stages[sidx], &full[sidx], cur);
-                next_claim = first + atomicAdd(A.tile_counter, 1);
             } else {
+                stage_tile[sidx] = -1;
                 mbar_arrive(&full[sidx]);   // releases the consumers: no tile
-                producing = false;
             }
-            ++nfills;
+            atomicAdd(nfills, 1u);
         }
-        // warp 0 reconverges after the producer's work, and leaves together
-        // with it if its wait ran out
-        if (__shfl_sync(0xffffffffu, (int)gave_up, 0)) break;
+        __syncwarp();
     }
-    // a wait ran out: the copies this CTA issued must land before it exits
-    if (tid == 0 && *abort_flag) drain_fills<NST>(full, nfills);
+    // A wait ran out: the copies this CTA issued must land before it exits.
+    // Every warp leaves the loop (each wait is bounded), so after the barrier
+    // no refill is in progress and the fills form a prefix of the sequence.
+    __syncthreads();
+    if (tid == 0 && *abort_flag) drain_fills<NST>(full, *nfills);
 }
 
 // 64 x 16 tiles, 3 stages, 256 threads, 2 CTAs per SM (128 registers).

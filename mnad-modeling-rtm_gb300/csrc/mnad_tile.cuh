@@ -64,6 +64,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity)
     return ok != 0;
 }
 
+// The same test without waiting (returns at once).
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, unsigned parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1)
 {
     asm volatile(
@@ -100,7 +114,11 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 __device__ __forceinline__ bool wait_bounded(uint64_t* bar, unsigned parity, const volatile int* abort_flag,
                                              const unsigned& limit)
 {
-    for (unsigned it = 0; it < limit; ++it) {
+    // The first poll does not wait (mbarrier.try_wait may itself wait until
+    // the phase completes), so a budget of one poll gives up on any phase
+    // still pending.
+    if (mbar_test_wait(bar, parity)) return true;
+    for (unsigned it = 1; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 1023u) == 1023u && *abort_flag) return false;
     }
