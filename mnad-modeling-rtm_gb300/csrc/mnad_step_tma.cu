@@ -5,21 +5,21 @@
 // propagation and origin).  Tiles are claimed dynamically from a per-launch
 // counter, since strip tiles cost more than interior ones.
 //
-// Each CTA keeps TMA_STAGES tiles in flight.  For a tile, thread 0 (the
-// producer) fills one shared-memory stage with a single mbarrier
-// transaction: 2-D bulk tensor copies of U, V, W of the current time level as
-// TMA_TZ+8 x TMA_TX+4 boxes (tile plus a 4-row / 2-column halo) and of pU, pV,
-// pW, r as TMA_TZ x TMA_TX boxes, plus 1-D bulk copies of the propagation's
-// descriptor and the tile's metadata.  Consumers (all TMA_THREADS threads,
-// thread 0 included) wait on that stage's "full" barrier, compute the tile
-// (each thread TMA_PZ consecutive z points of one column, a register window
-// along z; a warp covers two columns of TMA_TZ rows) and write nU, nV, nW
-// with vector stores over pU, pV, pW; each warp then
-// arrives on the stage's "empty" barrier.  Only the producer waits for
-// "empty" before refilling the stage, so no global-memory latency and no
-// CTA-wide barrier sits on the consumers' path; the producer's own tile
-// claim is an atomic issued one tile ahead.
-//
+// Each CTA keeps TMA_STAGES tiles in flight.  A stage is filled with a single
+// mbarrier transaction: one 3-D bulk tensor copy of U, V, W of the current
+// time level as a TMA_TZ+8 x TMA_TX+4 x 3 box (tile plus a 4-row / 2-column
+// halo), one of pU, pV, pW as a TMA_TZ x TMA_TX x 3 box, a 2-D copy of r,
+// and 1-D bulk copies of the propagation's descriptor and the tile's
+// metadata.  Consumers (all TMA_THREADS threads) wait on that stage's "full"
+// barrier, compute the tile (each thread TMA_PZ consecutive z points of one
+// column, a register window along z; a warp covers two columns of TMA_TZ
+// rows) and write nU, nV, nW with vector stores over pU, pV, pW.  Each warp
+// then counts itself in the stage's release count; the warp that completes
+// the count refills the stage with the tile thread 0 claimed for it one
+// iteration earlier.  So no global-memory latency and no CTA-wide barrier
+// sits on the consumers' path, and the producer work of a tile falls on the
+// warp that finished it last.
+
 // Interior points take a lean path; CPML strip points add the memory-
 // variable updates of Ux123_gen.m / Uz123_gen.m.
 //
