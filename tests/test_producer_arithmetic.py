@@ -10,6 +10,9 @@
   Replayed against a simulation of the producer's fill sequence.
 * A CTA's first NS tiles are b, b + grid, ... and later tiles are claimed
   from a counter offset by NS * grid: every tile is processed exactly once.
+* The last warp to release a stage refills it with the tile thread 0
+  claimed for that stage in the same iteration: replayed with warps moving
+  at random rates, every warp computes every tile of the CTA once, in order.
 No GPU is involved.
 """
 import numpy as np
@@ -66,3 +69,63 @@ def test_static_first_tiles_and_claims_cover_every_tile_once(ntiles, grid, ns):
         seen[first + counter] += 1
         counter += 1
     assert np.all(seen == 1)
+
+
+@pytest.mark.parametrize("nwarps,ns", [(8, 3), (4, 2)])
+@pytest.mark.parametrize("seed", range(6))
+def test_last_warp_refill_processes_each_claimed_tile_once_in_order(nwarps, ns, seed):
+    """Replay of the refill protocol with warps progressing at random rates:
+    thread 0 (warp 0) writes its claim for stage n % ns when it starts
+    iteration n; the warp that completes the release count of a stage
+    refills it with that claim; a warp may start iteration n only once the
+    stage holds iteration n's tile.  Every tile is then computed by every warp
+    exactly once, in claim order, and the stream ends with "no tile"."""
+    rng = np.random.default_rng(seed)
+    ntiles, grid, b = 50, 4, 1                       # one CTA (b) of a launch of `grid` CTAs
+    first = ns * grid
+    counter = iter(range(0, 10 ** 6))
+    claims_made = []
+
+    def claim():
+        t = first + next(counter) * grid + b         # the other CTAs take the claims in between
+        claims_made.append(t)
+        return t
+
+    stage_tile = [b + k * grid if b + k * grid < ntiles else -1 for k in range(ns)]
+    stage_iter = list(range(ns))                     # which iteration each stage currently serves
+    next_tile = [None] * ns
+    released = [0] * ns
+    next_claim = claim()
+    it = [0] * nwarps                                # next iteration of each warp
+    done = [False] * nwarps
+    computed = [[] for _ in range(nwarps)]
+    for _ in range(100000):
+        if all(done):
+            break
+        w = int(rng.integers(nwarps))
+        if done[w]:
+            continue
+        n = it[w]
+        s = n % ns
+        if stage_iter[s] != n:                       # the stage is not filled for this iteration yet
+            continue
+        t = stage_tile[s]
+        if t < 0:
+            done[w] = True
+            continue
+        if w == 0:                                   # thread 0: the claim for this stage's next fill
+            next_tile[s] = next_claim
+            next_claim = claim()
+        computed[w].append(t)
+        released[s] += 1
+        if released[s] == nwarps:                    # the last warp to release refills
+            assert next_tile[s] is not None          # written by warp 0 in this iteration
+            released[s] = 0
+            t2 = next_tile[s]
+            stage_tile[s] = t2 if t2 < ntiles else -1
+            stage_iter[s] = n + ns
+        it[w] += 1
+    assert all(done)
+    expected = [t for t in range(ntiles) if t % grid == b]
+    for w in range(nwarps):
+        assert computed[w] == expected
